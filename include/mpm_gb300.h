@@ -1,0 +1,222 @@
+/*
+ * mpm_gb300.h -- C ABI of the GB300 (sm_103a) MPM substep library
+ * (libmpm_gb300.so, built from reduced_mpm_stress_training_gb300/csrc).
+ *
+ * Drop-in boundary for MPM_Simulator_WARP.p2g2p of
+ * zeshunzong/reduced_mpm_stress_training (engine_stress/mpm_solver_warp.py).
+ * The reference reaches its device code through Warp's wp.launch with the
+ * by-value structs MPMModelStruct / MPMStateStruct (engine_stress/warp_utils.py:61-124);
+ * these entry points replace those launches.  Every function:
+ *   - takes plain pointers and sizes, no torch or Warp types;
+ *   - allocates no device memory: the caller owns every buffer
+ *     (sizes from mpm_plan);
+ *   - enqueues work on the given CUDA stream (cudaStream_t passed as void*,
+ *     NULL = legacy default stream) and does not synchronise it, except
+ *     where a host pointer is read or written (noted below);
+ *   - returns MPM_OK (0) or a negative MPM_ERR_* code.
+ * Physics faults (particles leaving the grid, CFL violation, non-finite
+ * F or stress) never trap: kernels OR a bit into the device status word
+ * (MpmBuffers.status) which the caller reads when it likes.
+ */
+#ifndef MPM_GB300_H
+#define MPM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPM_ABI_VERSION 1
+#define MPM_MAX_COLLIDERS 8
+
+/* return codes */
+#define MPM_OK 0
+#define MPM_ERR_ARG (-1)   /* bad argument (null pointer, size, field id)   */
+#define MPM_ERR_CUDA (-2)  /* a CUDA runtime call failed (launch, memcpy)   */
+#define MPM_ERR_SIZE (-3)  /* a size exceeds what the buffers were planned for */
+
+/* device status-word bits */
+#define MPM_ST_OUT_OF_DOMAIN 1 /* stencil outside [0,n-3]^3 or NaN position: particle frozen */
+#define MPM_ST_CFL 2           /* |v_i| > dx/dt (mpm_solver_warp.py:188-192)          */
+#define MPM_ST_NONFINITE 4     /* non-finite F or stress after the return map         */
+#define MPM_ST_INTERNAL 8      /* a particle was not inside its sorted block (bug)    */
+
+/* material ids, engine_stress/mpm_solver_warp.py:90-94 */
+#define MPM_JELLY 0
+#define MPM_METAL 1
+#define MPM_SAND 2
+
+/* collider kinds */
+#define MPM_COLLIDER_SURFACE 0 /* add_surface_collider, mpm_solver_warp.py:407-451 */
+#define MPM_COLLIDER_BOX 1     /* add_bounding_box,     mpm_solver_warp.py:499-525 */
+
+/* Dirichlet_collider subset used by the two grid boundary kernels
+ * (engine_stress/warp_utils.py:126-151).  normal must be unit length. */
+typedef struct MpmCollider {
+    int32_t kind;         /* MPM_COLLIDER_*                                      */
+    int32_t surface_type; /* 0 sticky, 1 slip, 2 separate; all three zero the
+                             node velocity, as the reference does (:449)         */
+    float point[3];
+    float normal[3];
+    float friction;
+    float start_time; /* active while start_time <= time < end_time */
+    float end_time;
+    float pad0;
+} MpmCollider; /* 48 bytes */
+
+/* One scene: MPMModelStruct (engine_stress/warp_utils.py:61-81) plus its
+ * particle range and grid-block range.  A plain simulator is one scene; the
+ * batched form concatenates many.  Fields marked (plan) are filled in by
+ * mpm_plan. */
+typedef struct MpmScene {
+    int32_t n_grid;    /* nodes per axis; grid covers [0, n_grid*dx)^3        */
+    int32_t material;  /* MPM_JELLY / MPM_METAL / MPM_SAND                   */
+    int32_t hardening; /* von Mises linear hardening on (1) / off (0)        */
+    int32_t n_colliders;
+    float dx, inv_dx;  /* grid_lim/n_grid and n_grid/grid_lim (:37)          */
+    float mu, lam;     /* Lame parameters                                    */
+    float alpha;       /* Drucker-Prager alpha from the friction angle (:113-116) */
+    float xi;          /* hardening slope                                    */
+    float gravity[3];  /* reference: (0, -g, 0) (mpm_utils.py:236)           */
+    int32_t n_blocks_axis;  /* (plan) ceil(n_grid/4)                          */
+    int64_t particle_begin; /* first particle (user order) of this scene     */
+    int64_t particle_count;
+    int64_t block_begin;    /* (plan) first global 4x4x4 grid-block id        */
+    MpmCollider colliders[MPM_MAX_COLLIDERS];
+} MpmScene; /* 464 bytes */
+
+/* Sizes computed by mpm_plan. */
+typedef struct MpmPlan {
+    int64_t n_particles;     /* total over all scenes                         */
+    int64_t particle_stride; /* padded per-field stride of the state (floats) */
+    int64_t total_blocks;    /* 4x4x4 grid blocks over all scenes             */
+    int64_t max_chunks;      /* upper bound of the per-substep work list      */
+    int64_t state_bytes;     /* bytes of ONE particle-state buffer             */
+    int64_t workspace_bytes; /* bytes of the workspace                         */
+    int32_t chunk_size;      /* particles per work chunk (32..256, power of 2) */
+    int32_t n_scenes;
+} MpmPlan; /* 56 bytes */
+
+/* Caller-owned device buffers plus the host-side control the library keeps
+ * between calls.  All pointers are device pointers (256-byte aligned). */
+typedef struct MpmBuffers {
+    void *state[2];   /* two particle-state buffers, plan.state_bytes each      */
+    void *workspace;  /* plan.workspace_bytes                                  */
+    void *scenes;     /* device copy of the MpmScene table (mpm_upload_scenes)  */
+    int32_t *status;  /* one device int32, MPM_ST_* bits, OR-accumulated        */
+    MpmPlan plan;
+    int32_t cur;             /* index of the live state buffer                  */
+    int32_t keys_valid;      /* 0 after a load that moves particles             */
+    int32_t resort_interval; /* physical re-sort every k substeps (0: only when
+                                keys were invalid)                              */
+    int32_t pad0;
+    int64_t substep;         /* substeps taken since mpm_init                   */
+} MpmBuffers;
+
+/* State fields for mpm_load / mpm_export.  Layout on the caller side is the
+ * reference's: AoS, user particle order, vec3 = 3 floats, mat33 = 9 floats
+ * row-major (engine_stress/warp_utils.py:5-43). */
+#define MPM_FIELD_X_INITIAL 0 /* vec3  particle_x_initial                     */
+#define MPM_FIELD_U 1         /* vec3  particle_u (displacement)               */
+#define MPM_FIELD_V 2         /* vec3  particle_v                              */
+#define MPM_FIELD_C 3         /* mat33 particle_C (APIC affine)                */
+#define MPM_FIELD_F 4         /* mat33 particle_F (elastic deformation grad.)  */
+#define MPM_FIELD_STRESS 5    /* mat33 particle_stress (Kirchhoff)             */
+#define MPM_FIELD_MASS 6      /* float particle_mass                           */
+#define MPM_FIELD_VOL 7       /* float particle_vol                            */
+#define MPM_FIELD_YIELD 8     /* float yield_stress (von Mises)                */
+#define MPM_FIELD_X 9         /* vec3  particle_x = x_initial + u   (export only) */
+#define MPM_FIELD_F_DISP 10   /* mat33 particle_F_disp = F - I      (export only) */
+
+/* ---- layout ---------------------------------------------------------- */
+
+/* Fill scenes[*].n_blocks_axis / block_begin and *plan for n_scenes scenes
+ * whose particle ranges tile [0, n_particles).  chunk_size 0 picks the
+ * default (128).  Host only.  Replaces the allocation half of
+ * MPM_Simulator_WARP.initialize (engine_stress/mpm_solver_warp.py:28-87). */
+int mpm_plan(MpmScene *scenes, int32_t n_scenes, int64_t n_particles, int32_t chunk_size,
+             MpmPlan *plan);
+
+/* Zero both state buffers and the workspace, set F = I and the identity
+ * particle order, clear the status word.  Replaces the initial values of
+ * MPM_Simulator_WARP.initialize (engine_stress/mpm_solver_warp.py:52-69). */
+int mpm_init(MpmBuffers *b, void *stream);
+
+/* Copy n_scenes host MpmScene records into b->scenes (stream-ordered; reads
+ * the host table before returning).  Replaces the by-value MPMModelStruct
+ * argument of every wp.launch (engine_stress/mpm_solver_warp.py:157-197) and
+ * set_parameters (:89-127) / add_surface_collider (:407) / add_bounding_box (:499). */
+int mpm_upload_scenes(MpmBuffers *b, const MpmScene *scenes, int32_t n_scenes, void *stream);
+
+/* ---- particle data in the reference layout --------------------------- */
+
+/* Load one field for all particles from src (reference layout, user order).
+ * src_on_host != 0: src is host memory (pinned for asynchrony) and is copied
+ * through the workspace.  Replaces load_x_initial_from_tensor (:229-230),
+ * load_mass_from_tensor (:231-232), load_uvF_from_tensor (:234-245),
+ * load_C_from_tensor (:247-251), load_uvstress_from_tensor (:253-266) and the
+ * set_value kernels of set_parameters (:108-124). */
+int mpm_load(MpmBuffers *b, int32_t field, const float *src, int32_t src_on_host, void *stream);
+
+/* Export one field for all particles to dst (reference layout, user order).
+ * dst_on_host != 0: dst is host memory; the call then waits for the copy.
+ * Replaces export_uvFstress_from_warp (:305-310) and the wp.array reads of
+ * mpm_state.particle_* (e.g. save_data_at_frame :351-384). */
+int mpm_export(MpmBuffers *b, int32_t field, float *dst, int32_t dst_on_host, void *stream);
+
+/* ---- the substep ----------------------------------------------------- */
+
+/* One full substep for every scene: x = x0 + u, cell-block sort, APIC P2G
+ * with the stored stress, grid normalisation + gravity + colliders, G2P with
+ * APIC C, F update, return mapping and Kirchhoff stress, u = x - x0.
+ * `time` gates the colliders.  Replaces MPM_Simulator_WARP.p2g2p
+ * (engine_stress/mpm_solver_warp.py:156-203), i.e. the launches of
+ * update_x_from_u, zero_grid, p2g_apic_stress_given,
+ * grid_normalization_and_gravity, the collider kernels, g2p_apic_and_stress,
+ * update_u_from_x and update_F_disp_from_F (engine_stress/mpm_utils.py). */
+int mpm_p2g2p(MpmBuffers *b, float time, float dt, void *stream);
+
+/* The substep's stages, for callers that interleave their own work and for
+ * per-stage checks.  mpm_p2g2p == sort, p2g, grid_update, g2p. */
+int mpm_sort(MpmBuffers *b, void *stream); /* block keys, counting sort, re-sort */
+int mpm_p2g(MpmBuffers *b, float dt, void *stream); /* mpm_utils.py:190-227 */
+int mpm_grid_update(MpmBuffers *b, float time, float dt, void *stream); /* :229-237 + colliders */
+int mpm_g2p(MpmBuffers *b, float dt, void *stream); /* mpm_utils.py:241-306, :4-19 */
+
+/* Dense (n,n,n) C-order copy of one scene's grid after the last stage that
+ * wrote it: grid_m and grid_v_in (momentum) are valid between mpm_p2g and
+ * mpm_grid_update, grid_v_out after mpm_grid_update.  Untouched nodes read 0,
+ * as after the reference's zero_grid.  Any pointer may be NULL.  Replaces
+ * reads of mpm_state.grid_m / grid_v_in / grid_v_out (warp_utils.py:109-112). */
+int mpm_export_grid(MpmBuffers *b, int32_t scene, float *grid_m, float *grid_v_in,
+                    float *grid_v_out, void *stream);
+
+/* ---- element kernels on plain arrays --------------------------------- */
+
+/* Batched 3x3 SVD, A (n,9) row-major -> U (n,9), s (n,3), V (n,9):
+ * U, V rotations, |s| descending, sign(det A) on s[2].  Replaces wp.svd3
+ * (called at engine_stress/mpm_utils.py:64, :92, :297). */
+int mpm_svd3(const float *A, float *U, float *s, float *V, int64_t n, void *stream);
+
+/* Batched return mapping + Kirchhoff stress of one scene's material:
+ * F_trial (n,9) -> F (n,9), stress (n,9); yield (n) read and, with
+ * hardening, updated (may be NULL unless the material is metal).
+ * Replaces von_mises_return_mapping / sand_return_mapping and the stress
+ * functions (engine_stress/mpm_utils.py:29-112, :284-306). */
+int mpm_return_map(const MpmScene *scene, const float *F_trial, float *yield, float *F,
+                   float *stress, int64_t n, void *stream);
+
+/* ---- misc ------------------------------------------------------------ */
+int mpm_abi_version(void);
+/* sizeof of the ABI structs, for binding checks: out[0..3] =
+ * MpmCollider, MpmScene, MpmPlan, MpmBuffers. */
+void mpm_struct_sizes(int64_t *out);
+const char *mpm_error_string(int code);
+/* Last CUDA error text seen by the library on this host thread ("" if none). */
+const char *mpm_last_cuda_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPM_GB300_H */

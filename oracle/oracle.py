@@ -1,0 +1,256 @@
+"""ctypes front end of the CPU oracle (test infrastructure, not product).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs use
+this module; it is the checker, never the thing measured for the GPU path.
+
+``OracleSim`` holds the reference's own arrays (engine_stress/mpm_solver_warp.py:52-69:
+AoS vec3 / row-major mat33 per particle, dense (n,n,n) grid) as NumPy arrays
+in float32 or float64 and advances them with the C restatement in
+``mpm_oracle.c``.  Parity is unpinned against the reference itself (no
+golden vectors exist and Warp is not installed); see ``mpm_oracle.c``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import build as _build
+
+ST_OUT_OF_DOMAIN = 1
+ST_CFL = 2
+ST_NONFINITE = 4
+
+
+class OrcModel(C.Structure):
+    _fields_ = [
+        ("n_grid", C.c_int32),
+        ("material", C.c_int32),
+        ("hardening", C.c_int32),
+        ("pad0", C.c_int32),
+        ("dx", C.c_double),
+        ("inv_dx", C.c_double),
+        ("mu", C.c_double),
+        ("lam", C.c_double),
+        ("alpha", C.c_double),
+        ("xi", C.c_double),
+        ("gravity", C.c_double * 3),
+    ]
+
+
+class OrcCollider(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("surface_type", C.c_int32),
+        ("point", C.c_double * 3),
+        ("normal", C.c_double * 3),
+        ("friction", C.c_double),
+        ("start_time", C.c_double),
+        ("end_time", C.c_double),
+    ]
+
+
+_STATE_FIELDS = ["x0", "x", "u", "v", "C", "F", "F_trial", "F_disp", "stress", "mass", "vol",
+                 "yield_", "grid_m", "grid_v_in", "grid_v_out"]
+
+_libs: dict[int, C.CDLL] = {}
+
+
+def lib(bits: int) -> C.CDLL:
+    if bits not in _libs:
+        _build.build()
+        _libs[bits] = C.CDLL(_build.lib_path(bits))
+    return _libs[bits]
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.flags.c_contiguous
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def max_threads() -> int:
+    f = lib(32).orc32_max_threads
+    f.restype = C.c_int
+    return int(f())
+
+
+def material_code(material: str) -> int:
+    """engine_stress/mpm_solver_warp.py:90-94"""
+    codes = {"jelly": 0, "metal": 1, "sand": 2}
+    if material not in codes:
+        raise TypeError("Undefined material type")
+    return codes[material]
+
+
+def make_model(n_grid: int, grid_lim: float = 1.0, material: str = "sand", E: float | None = None,
+               nu: float | None = None, mu: float | None = None, lam: float | None = None,
+               friction_angle: float = 25.0, gravity=(0.0, 0.0, 0.0), hardening: int = 0,
+               xi: float = 0.0) -> OrcModel:
+    """Parameter conversions of engine_stress/mpm_solver_warp.py:37-48, :101, :113-116."""
+    m = OrcModel()
+    m.n_grid = n_grid
+    m.material = material_code(material)
+    m.hardening = hardening
+    m.dx = grid_lim / n_grid
+    m.inv_dx = float(n_grid / grid_lim)
+    if E is not None:
+        nu = 0.3 if nu is None else nu
+        mu = E / 2.0 / (1.0 + nu)
+        lam = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu)
+    m.mu = mu
+    m.lam = lam
+    sin_phi = math.sin(friction_angle / 180.0 * 3.14159265)
+    m.alpha = math.sqrt(2.0 / 3.0) * 2.0 * sin_phi / (3.0 - sin_phi)
+    m.xi = xi
+    for c in range(3):
+        m.gravity[c] = gravity[c]
+    return m
+
+
+def surface_collider(point, normal, surface="sticky", friction=0.0, start_time=0.0,
+                     end_time=999.0) -> OrcCollider:
+    """engine_stress/mpm_solver_warp.py:407-428"""
+    col = OrcCollider()
+    col.kind = 0
+    scale = 1.0 / math.sqrt(sum(x * x for x in normal))
+    for c in range(3):
+        col.point[c] = point[c]
+        col.normal[c] = scale * normal[c]
+    if surface == "sticky" and friction != 0:
+        raise ValueError("friction must be 0 on sticky surfaces.")
+    col.surface_type = 0 if surface == "sticky" else (1 if surface == "slip" else 2)
+    col.friction = friction
+    col.start_time = start_time
+    col.end_time = end_time
+    return col
+
+
+def bounding_box(start_time=0.0, end_time=999.0) -> OrcCollider:
+    """engine_stress/mpm_solver_warp.py:499-503"""
+    col = OrcCollider()
+    col.kind = 1
+    col.start_time = start_time
+    col.end_time = end_time
+    return col
+
+
+class OracleSim:
+    """Reference-layout simulator state advanced by the C oracle."""
+
+    def __init__(self, model: OrcModel, x0: np.ndarray, mass: np.ndarray, vol: np.ndarray,
+                 v: np.ndarray | None = None, bits: int = 32, colliders=(), yield_stress=None):
+        self.bits = bits
+        self.dtype = np.float32 if bits == 32 else np.float64
+        self.model = model
+        self.colliders = list(colliders)
+        n = x0.shape[0]
+        self.n = n
+        dt = self.dtype
+        ng = model.n_grid
+        self.x0 = np.ascontiguousarray(x0, dtype=dt).reshape(n, 3)
+        self.x = self.x0.copy()
+        self.u = np.zeros((n, 3), dt)
+        self.v = np.zeros((n, 3), dt) if v is None else np.ascontiguousarray(v, dtype=dt).reshape(n, 3).copy()
+        self.C = np.zeros((n, 9), dt)
+        self.F = np.tile(np.eye(3, dtype=dt).reshape(1, 9), (n, 1))
+        self.F_trial = np.zeros((n, 9), dt)
+        self.F_disp = np.zeros((n, 9), dt)
+        self.stress = np.zeros((n, 9), dt)
+        self.mass = np.ascontiguousarray(mass, dtype=dt).reshape(n).copy()
+        self.vol = np.ascontiguousarray(vol, dtype=dt).reshape(n).copy()
+        ys = 0.0 if yield_stress is None else yield_stress
+        self.yield_ = np.broadcast_to(np.asarray(ys, dtype=dt), (n,)).copy()
+        self.grid_m = np.zeros((ng, ng, ng), dt)
+        self.grid_v_in = np.zeros((ng, ng, ng, 3), dt)
+        self.grid_v_out = np.zeros((ng, ng, ng, 3), dt)
+        self.time = 0.0
+        self.status = C.c_int32(0)
+
+    def _fn(self, name):
+        return getattr(lib(self.bits), f"orc{self.bits}_{name}")
+
+    def _state(self):
+        bits = self.bits
+
+        class State(C.Structure):
+            _fields_ = [(f, C.c_void_p) for f in _STATE_FIELDS]
+
+        s = State()
+        for f in _STATE_FIELDS:
+            setattr(s, f, _ptr(getattr(self, f)).value)
+        return s
+
+    def _real(self, x):
+        return C.c_float(x) if self.bits == 32 else C.c_double(x)
+
+    def p2g2p(self, dt: float, nthreads_p2g: int = 1) -> None:
+        """One substep, engine_stress/mpm_solver_warp.py:156-199 (time += dt)."""
+        s = self._state()
+        ncol = len(self.colliders)
+        arr = (OrcCollider * max(ncol, 1))(*self.colliders)
+        self._fn("p2g2p")(C.byref(self.model), C.byref(s), C.c_int64(self.n), arr, C.c_int(ncol),
+                          C.c_double(self.time), self._real(dt), C.c_int(nthreads_p2g),
+                          C.byref(self.status))
+        self.time = self.time + dt
+
+    # ---- individual kernels (same order as p2g2p) for per-stage checks ----
+    def stage_p2g(self, dt: float) -> None:
+        nn = self.model.n_grid ** 3
+        self._fn("update_x_from_u")(C.c_int64(self.n), _ptr(self.x0), _ptr(self.u), _ptr(self.x))
+        self._fn("zero_grid")(C.c_int64(nn), _ptr(self.grid_m), _ptr(self.grid_v_in),
+                              _ptr(self.grid_v_out))
+        self._fn("p2g_apic_stress_given")(C.byref(self.model), C.c_int64(self.n), _ptr(self.x),
+                                          _ptr(self.v), _ptr(self.C), _ptr(self.stress),
+                                          _ptr(self.mass), _ptr(self.vol), self._real(dt),
+                                          _ptr(self.grid_m), _ptr(self.grid_v_in),
+                                          C.byref(self.status), C.c_int(1))
+
+    def stage_grid(self, dt: float) -> None:
+        self._fn("grid_normalization_and_gravity")(C.byref(self.model), self._real(dt),
+                                                   _ptr(self.grid_m), _ptr(self.grid_v_in),
+                                                   _ptr(self.grid_v_out))
+        for col in self.colliders:
+            name = "collide_surface" if col.kind == 0 else "collide_bounding_box"
+            self._fn(name)(C.byref(self.model), C.byref(col), C.c_double(self.time),
+                           _ptr(self.grid_v_out))
+
+    def stage_g2p(self, dt: float) -> None:
+        self._fn("g2p_apic_and_stress")(C.byref(self.model), C.c_int64(self.n), self._real(dt),
+                                        _ptr(self.grid_v_out), _ptr(self.x), _ptr(self.v),
+                                        _ptr(self.C), _ptr(self.F_trial), _ptr(self.F),
+                                        _ptr(self.stress), _ptr(self.yield_),
+                                        C.byref(self.status))
+        self._fn("update_u_from_x")(C.c_int64(self.n), _ptr(self.x), _ptr(self.x0), _ptr(self.u))
+        self._fn("update_F_disp_from_F")(C.c_int64(self.n), _ptr(self.F), _ptr(self.F_disp))
+        self.time = self.time + dt
+
+
+def svd3(A: np.ndarray, bits: int = 32):
+    """Batch 3x3 SVD with the oracle's convention. A: (n, 9) or (n,3,3)."""
+    dt = np.float32 if bits == 32 else np.float64
+    A = np.ascontiguousarray(A, dtype=dt).reshape(-1, 9)
+    n = A.shape[0]
+    U = np.zeros((n, 9), dt)
+    s = np.zeros((n, 3), dt)
+    V = np.zeros((n, 9), dt)
+    getattr(lib(bits), f"orc{bits}_svd3_batch")(C.c_int64(n), _ptr(A), _ptr(U), _ptr(s), _ptr(V))
+    return U.reshape(n, 3, 3), s, V.reshape(n, 3, 3)
+
+
+def return_map(model: OrcModel, F_trial: np.ndarray, yield_stress=None, bits: int = 32):
+    """Return map + Kirchhoff stress as g2p_apic_and_stress does (mpm_utils.py:284-306)."""
+    dt = np.float32 if bits == 32 else np.float64
+    Ft = np.ascontiguousarray(F_trial, dtype=dt).reshape(-1, 9)
+    n = Ft.shape[0]
+    Fo = np.zeros((n, 9), dt)
+    tau = np.zeros((n, 9), dt)
+    y = None
+    if yield_stress is not None:
+        y = np.broadcast_to(np.asarray(yield_stress, dt), (n,)).copy()
+    getattr(lib(bits), f"orc{bits}_return_map_batch")(C.byref(model), C.c_int64(n), _ptr(Ft),
+                                                      _ptr(y), _ptr(Fo), _ptr(tau))
+    return Fo, tau, y

@@ -1,0 +1,324 @@
+// C ABI of libmpm_gb300.so (declared in include/mpm_gb300.h): buffer layout,
+// argument checks, and the launch sequence of the substep.
+#include <stdio.h>
+#include <string.h>
+
+#include "mpm_launch.h"
+
+namespace {
+
+thread_local char g_cuda_err[256] = "";
+
+int fail_cuda(cudaError_t e) {
+    snprintf(g_cuda_err, sizeof(g_cuda_err), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+    return MPM_ERR_CUDA;
+}
+
+#define MPM_CHECK(expr)                          \
+    do {                                         \
+        cudaError_t e_ = (expr);                 \
+        if (e_ != cudaSuccess) return fail_cuda(e_); \
+    } while (0)
+
+int num_sms() {
+    static int cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+    if (cache[dev] == 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+            v = 148;
+        cache[dev] = v;
+    }
+    return cache[dev];
+}
+
+constexpr int64_t kAlign = 256;
+inline int64_t align_up(int64_t x, int64_t a = kAlign) { return (x + a - 1) / a * a; }
+
+// particle-state buffer: 39 float arrays then uid and key, each `stride` long
+constexpr int kStateFloatArrays = 3 + 3 + 3 + 9 + 9 + 9 + 1 + 1 + 1;  // 39
+constexpr int kStateArrays = kStateFloatArrays + 2;
+
+struct WsLayout {
+    int64_t order, counts, offsets, cursor, tile_sums, ticket, chunks, n_chunks, grid_acc, grid_v,
+        block_flag, active_list, n_active, n_active_prev, staging, total;
+    int nbk, n_tiles;
+};
+
+WsLayout ws_layout(const MpmPlan &p) {
+    WsLayout L;
+    const int64_t n = p.particle_stride;
+    const int64_t nbk = p.total_blocks + 1;
+    L.nbk = (int)nbk;
+    L.n_tiles = (int)((nbk + mpm::kScanTile - 1) / mpm::kScanTile);
+    int64_t o = 0;
+    auto take = [&](int64_t bytes) { int64_t at = o; o = align_up(o + bytes); return at; };
+    L.order = take(n * 4);
+    L.counts = take(nbk * 4);
+    L.offsets = take(nbk * 4);
+    L.cursor = take(nbk * 4);
+    L.tile_sums = take((int64_t)L.n_tiles * 8);
+    L.ticket = take(4);
+    L.chunks = take(p.max_chunks * 16);
+    L.n_chunks = take(4);
+    L.grid_acc = take(p.total_blocks * mpm::kBlockNodes * 16);
+    L.grid_v = take(p.total_blocks * mpm::kBlockNodes * 16);
+    L.block_flag = take(p.total_blocks * 4);
+    L.active_list = take(p.total_blocks * 4);
+    L.n_active = take(4);
+    L.n_active_prev = take(4);
+    L.staging = take(n * 9 * 4);
+    L.total = o;
+    return L;
+}
+
+mpm::PState state_view(void *base, int64_t stride) {
+    float *f = static_cast<float *>(base);
+    mpm::PState s;
+    s.stride = stride;
+    s.x0 = f;
+    s.u = f + 3 * stride;
+    s.v = f + 6 * stride;
+    s.C = f + 9 * stride;
+    s.F = f + 18 * stride;
+    s.tau = f + 27 * stride;
+    s.mass = f + 36 * stride;
+    s.vol = f + 37 * stride;
+    s.yld = f + 38 * stride;
+    s.uid = reinterpret_cast<int *>(f + 39 * stride);
+    s.key = reinterpret_cast<int *>(f + 40 * stride);
+    return s;
+}
+
+mpm::Ctx make_ctx(const MpmBuffers *b, void *stream, int which) {
+    const MpmPlan &p = b->plan;
+    WsLayout L = ws_layout(p);
+    char *w = static_cast<char *>(b->workspace);
+    mpm::Ctx cx;
+    cx.scenes = static_cast<const MpmScene *>(b->scenes);
+    cx.n_scenes = p.n_scenes;
+    cx.st = state_view(b->state[which], p.particle_stride);
+    mpm::Ws &ws = cx.ws;
+    ws.order = reinterpret_cast<int *>(w + L.order);
+    ws.counts = reinterpret_cast<int *>(w + L.counts);
+    ws.offsets = reinterpret_cast<int *>(w + L.offsets);
+    ws.cursor = reinterpret_cast<int *>(w + L.cursor);
+    ws.tile_sums = reinterpret_cast<int2 *>(w + L.tile_sums);
+    ws.ticket = reinterpret_cast<unsigned *>(w + L.ticket);
+    ws.chunks = reinterpret_cast<int4 *>(w + L.chunks);
+    ws.n_chunks = reinterpret_cast<int *>(w + L.n_chunks);
+    ws.grid_acc = reinterpret_cast<float4 *>(w + L.grid_acc);
+    ws.grid_v = reinterpret_cast<float4 *>(w + L.grid_v);
+    ws.block_flag = reinterpret_cast<int *>(w + L.block_flag);
+    ws.active_list = reinterpret_cast<int *>(w + L.active_list);
+    ws.n_active = reinterpret_cast<int *>(w + L.n_active);
+    ws.n_active_prev = reinterpret_cast<int *>(w + L.n_active_prev);
+    ws.staging = reinterpret_cast<float *>(w + L.staging);
+    ws.nbk = L.nbk;
+    ws.n_tiles = L.n_tiles;
+    ws.max_chunks = (int)p.max_chunks;
+    ws.chunk_size = p.chunk_size;
+    cx.n = (int)p.n_particles;
+    cx.status = b->status;
+    cx.stream = static_cast<cudaStream_t>(stream);
+    cx.num_sms = num_sms();
+    cx.total_blocks = p.total_blocks;
+    return cx;
+}
+
+bool buffers_ok(const MpmBuffers *b) {
+    return b && b->state[0] && b->state[1] && b->workspace && b->scenes && b->status &&
+           b->plan.n_scenes >= 1 && (b->cur == 0 || b->cur == 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpm_abi_version(void) { return MPM_ABI_VERSION; }
+
+void mpm_struct_sizes(int64_t *out) {
+    if (!out) return;
+    out[0] = sizeof(MpmCollider);
+    out[1] = sizeof(MpmScene);
+    out[2] = sizeof(MpmPlan);
+    out[3] = sizeof(MpmBuffers);
+}
+
+const char *mpm_error_string(int code) {
+    switch (code) {
+        case MPM_OK: return "ok";
+        case MPM_ERR_ARG: return "invalid argument";
+        case MPM_ERR_CUDA: return "CUDA runtime error";
+        case MPM_ERR_SIZE: return "size exceeds the planned buffers";
+        default: return "unknown error";
+    }
+}
+
+const char *mpm_last_cuda_error(void) { return g_cuda_err; }
+
+int mpm_plan(MpmScene *scenes, int32_t n_scenes, int64_t n_particles, int32_t chunk_size,
+             MpmPlan *plan) {
+    if (!scenes || !plan || n_scenes < 1 || n_particles < 0) return MPM_ERR_ARG;
+    if (chunk_size == 0) chunk_size = 128;
+    if (chunk_size != 32 && chunk_size != 64 && chunk_size != 128 && chunk_size != 256)
+        return MPM_ERR_ARG;
+    if (n_particles >= (int64_t)1 << 30) return MPM_ERR_SIZE;
+    int64_t next_particle = 0, blocks = 0;
+    for (int s = 0; s < n_scenes; ++s) {
+        MpmScene &S = scenes[s];
+        if (S.n_grid < 3 || S.n_grid > 4096 || !(S.dx > 0.0f) || !(S.inv_dx > 0.0f)) return MPM_ERR_ARG;
+        if (S.material < MPM_JELLY || S.material > MPM_SAND) return MPM_ERR_ARG;
+        if (S.n_colliders < 0 || S.n_colliders > MPM_MAX_COLLIDERS) return MPM_ERR_ARG;
+        if (S.particle_begin != next_particle || S.particle_count < 0) return MPM_ERR_ARG;
+        next_particle += S.particle_count;
+        S.n_blocks_axis = (S.n_grid + 3) / 4;
+        S.block_begin = blocks;
+        blocks += (int64_t)S.n_blocks_axis * S.n_blocks_axis * S.n_blocks_axis;
+    }
+    if (next_particle != n_particles) return MPM_ERR_ARG;
+    if (blocks >= ((int64_t)1 << 31) / mpm::kBlockNodes) return MPM_ERR_SIZE;
+    MpmPlan p;
+    memset(&p, 0, sizeof(p));
+    p.n_particles = n_particles;
+    p.particle_stride = align_up(n_particles > 0 ? n_particles : 1, 64);
+    p.total_blocks = blocks;
+    p.chunk_size = chunk_size;
+    p.n_scenes = n_scenes;
+    const int64_t nonempty = n_particles < blocks ? n_particles : blocks;
+    p.max_chunks = n_particles / chunk_size + nonempty + 1;
+    p.state_bytes = (int64_t)kStateArrays * p.particle_stride * 4;
+    p.workspace_bytes = ws_layout(p).total;
+    *plan = p;
+    return MPM_OK;
+}
+
+int mpm_init(MpmBuffers *b, void *stream) {
+    if (!buffers_ok(b)) return MPM_ERR_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    MPM_CHECK(cudaMemsetAsync(b->state[0], 0, b->plan.state_bytes, st));
+    MPM_CHECK(cudaMemsetAsync(b->state[1], 0, b->plan.state_bytes, st));
+    MPM_CHECK(cudaMemsetAsync(b->workspace, 0, b->plan.workspace_bytes, st));
+    MPM_CHECK(cudaMemsetAsync(b->status, 0, sizeof(int32_t), st));
+    b->cur = 0;
+    b->keys_valid = 0;
+    b->substep = 0;
+    mpm::Ctx cx = make_ctx(b, stream, 0);
+    mpm::PState other = state_view(b->state[1], b->plan.particle_stride);
+    MPM_CHECK(mpm::launch_init_state(cx, other));
+    return MPM_OK;
+}
+
+int mpm_upload_scenes(MpmBuffers *b, const MpmScene *scenes, int32_t n_scenes, void *stream) {
+    if (!b || !b->scenes || !scenes || n_scenes != b->plan.n_scenes) return MPM_ERR_ARG;
+    MPM_CHECK(cudaMemcpyAsync(b->scenes, scenes, sizeof(MpmScene) * (size_t)n_scenes,
+                              cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
+int mpm_load(MpmBuffers *b, int32_t field, const float *src, int32_t src_on_host, void *stream) {
+    if (!buffers_ok(b) || (!src && b->plan.n_particles > 0) || field < MPM_FIELD_X_INITIAL ||
+        field > MPM_FIELD_YIELD)
+        return MPM_ERR_ARG;
+    mpm::Ctx cx = make_ctx(b, stream, b->cur);
+    const float *from = src;
+    if (src_on_host) {
+        size_t bytes = (size_t)cx.n * mpm::field_components(field) * sizeof(float);
+        if (bytes) MPM_CHECK(cudaMemcpyAsync(cx.ws.staging, src, bytes, cudaMemcpyHostToDevice, cx.stream));
+        from = cx.ws.staging;
+    }
+    MPM_CHECK(mpm::launch_load(cx, field, from));
+    if (field == MPM_FIELD_X_INITIAL || field == MPM_FIELD_U) b->keys_valid = 0;
+    return MPM_OK;
+}
+
+int mpm_export(MpmBuffers *b, int32_t field, float *dst, int32_t dst_on_host, void *stream) {
+    if (!buffers_ok(b) || (!dst && b->plan.n_particles > 0) || field < MPM_FIELD_X_INITIAL ||
+        field > MPM_FIELD_F_DISP)
+        return MPM_ERR_ARG;
+    mpm::Ctx cx = make_ctx(b, stream, b->cur);
+    float *to = dst_on_host ? cx.ws.staging : dst;
+    MPM_CHECK(mpm::launch_export(cx, field, to));
+    if (dst_on_host) {
+        size_t bytes = (size_t)cx.n * mpm::field_components(field) * sizeof(float);
+        if (bytes) MPM_CHECK(cudaMemcpyAsync(dst, to, bytes, cudaMemcpyDeviceToHost, cx.stream));
+        MPM_CHECK(cudaStreamSynchronize(cx.stream));
+    }
+    return MPM_OK;
+}
+
+int mpm_sort(MpmBuffers *b, void *stream) {
+    if (!buffers_ok(b)) return MPM_ERR_ARG;
+    mpm::Ctx cx = make_ctx(b, stream, b->cur);
+    bool resort = false;
+    if (!b->keys_valid) {
+        MPM_CHECK(cudaMemsetAsync(cx.ws.counts, 0, (size_t)cx.ws.nbk * sizeof(int), cx.stream));
+        MPM_CHECK(mpm::launch_keys(cx));
+        b->keys_valid = 1;
+        resort = true;
+    }
+    MPM_CHECK(mpm::launch_sort(cx));
+    if (b->resort_interval > 0 && b->substep % b->resort_interval == 0) resort = true;
+    if (resort) {
+        mpm::PState dst = state_view(b->state[b->cur ^ 1], b->plan.particle_stride);
+        MPM_CHECK(mpm::launch_permute(cx, dst));
+        b->cur ^= 1;
+    }
+    return MPM_OK;
+}
+
+int mpm_p2g(MpmBuffers *b, float dt, void *stream) {
+    if (!buffers_ok(b)) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_p2g(make_ctx(b, stream, b->cur), dt));
+    return MPM_OK;
+}
+
+int mpm_grid_update(MpmBuffers *b, float time, float dt, void *stream) {
+    if (!buffers_ok(b)) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_grid(make_ctx(b, stream, b->cur), time, dt));
+    return MPM_OK;
+}
+
+int mpm_g2p(MpmBuffers *b, float dt, void *stream) {
+    if (!buffers_ok(b)) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_g2p(make_ctx(b, stream, b->cur), dt));
+    b->substep += 1;
+    return MPM_OK;
+}
+
+int mpm_p2g2p(MpmBuffers *b, float time, float dt, void *stream) {
+    int r = mpm_sort(b, stream);
+    if (r) return r;
+    if ((r = mpm_p2g(b, dt, stream))) return r;
+    if ((r = mpm_grid_update(b, time, dt, stream))) return r;
+    return mpm_g2p(b, dt, stream);
+}
+
+int mpm_export_grid(MpmBuffers *b, int32_t scene, float *grid_m, float *grid_v_in,
+                    float *grid_v_out, void *stream) {
+    if (!buffers_ok(b) || scene < 0 || scene >= b->plan.n_scenes) return MPM_ERR_ARG;
+    mpm::Ctx cx = make_ctx(b, stream, b->cur);
+    MpmScene S;
+    MPM_CHECK(cudaMemcpyAsync(&S, cx.scenes + scene, sizeof(S), cudaMemcpyDeviceToHost, cx.stream));
+    MPM_CHECK(cudaStreamSynchronize(cx.stream));
+    MPM_CHECK(mpm::launch_export_grid(cx, S, scene, grid_m, grid_v_in, grid_v_out));
+    return MPM_OK;
+}
+
+int mpm_svd3(const float *A, float *U, float *s, float *V, int64_t n, void *stream) {
+    if (n < 0 || (n > 0 && (!A || !U || !s || !V))) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_svd3(A, U, s, V, n, static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
+int mpm_return_map(const MpmScene *scene, const float *F_trial, float *yield, float *F,
+                   float *stress, int64_t n, void *stream) {
+    if (!scene || n < 0 || (n > 0 && (!F_trial || !F || !stress))) return MPM_ERR_ARG;
+    if (scene->material == MPM_METAL && n > 0 && !yield) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_return_map(*scene, F_trial, yield, F, stress, n,
+                                     static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
+}  // extern "C"

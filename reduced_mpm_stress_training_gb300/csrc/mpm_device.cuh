@@ -1,0 +1,361 @@
+// Device-side building blocks shared by the substep kernels: buffer views,
+// the stencil set-up, the 3x3 SVD, and the fused return map + Kirchhoff
+// stress.  Every function here states the reference lines it follows.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mpm_gb300.h"
+
+namespace mpm {
+
+constexpr int kTile = 6;                // padded node tile per 4^3-cell block
+constexpr int kTileNodes = kTile * kTile * kTile;  // 216
+constexpr int kBlockNodes = 64;         // nodes of one 4x4x4 grid block
+constexpr int kScanTile = 2048;         // buckets per scan CTA (256 threads x 8)
+constexpr int kSvdSweeps = 5;           // Jacobi sweeps (converged in float32)
+
+// ---------------------------------------------------------------------------
+// Views of the caller's buffers (layout fixed by mpm_plan).
+// ---------------------------------------------------------------------------
+struct PState {  // one particle-state buffer, SoA, component stride `stride`
+    float *x0, *u, *v, *C, *F, *tau, *mass, *vol, *yld;
+    int *uid;  // user index of each slot
+    int *key;  // grid-block key of each slot for the coming sort
+    int64_t stride;
+};
+
+struct Ws {  // workspace
+    int *order, *counts, *offsets, *cursor;
+    int2 *tile_sums;
+    unsigned *ticket;
+    int4 *chunks;     // (global block, start, count, scene)
+    int *n_chunks;
+    float4 *grid_acc; // (momentum xyz, mass), block-major
+    float4 *grid_v;   // (velocity xyz, mass) after the grid update
+    int *block_flag;
+    int *active_list;
+    int *n_active;
+    int *n_active_prev;  // active blocks of the previous substep (to clear)
+    float *staging;
+    int nbk;          // buckets = total_blocks + 1 (last = out of domain)
+    int n_tiles;
+    int max_chunks;
+    int chunk_size;
+};
+
+// ---------------------------------------------------------------------------
+// Stencil set-up, engine_stress/mpm_utils.py:196-209 and :244-257.
+// Explicit _rn intrinsics keep these roundings free of FMA contraction so the
+// key computed at the end of G2P and the base recomputed by the next P2G are
+// bit-identical (and equal to the reference's x*inv_dx, int(gp-0.5), gp-base).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float grid_coord(float x0, float u, float inv_dx) {
+    return __fmul_rn(__fadd_rn(x0, u), inv_dx);  // x = x0 + u (:5-7), gp = x * inv_dx
+}
+
+// base index of one axis; returns false when the 3-node stencil would leave
+// [0, n-1] or gp is NaN (the reference does not check; we flag and skip).
+__device__ __forceinline__ bool stencil_base(float gp, int n, int &base) {
+    float t = __fsub_rn(gp, 0.5f);
+    bool ok = (t > -1.0f) && (t < (float)(n - 2));
+    base = ok ? (int)t : 0;  // wp.int truncates toward zero
+    return ok;
+}
+
+struct Weights {
+    float w[3][3];   // w[axis][node offset]
+    float dw[3][3];  // derivative wrt fx (times inv_dx gives the gradient)
+    float fx[3];
+};
+
+__device__ __forceinline__ void make_weights(const float gp[3], const int base[3], Weights &W) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float fx = __fsub_rn(gp[d], (float)base[d]);
+        W.fx[d] = fx;
+        float wa = 1.5f - fx, wb = fx - 1.0f, wc = fx - 0.5f;
+        W.w[d][0] = wa * wa * 0.5f;
+        W.w[d][1] = (0.0f - wb * wb) + 0.75f;
+        W.w[d][2] = wc * wc * 0.5f;
+        W.dw[d][0] = fx - 1.5f;
+        W.dw[d][1] = -2.0f * (fx - 1.0f);
+        W.dw[d][2] = fx - 0.5f;
+    }
+}
+
+// global node index in the block-major grid of one scene
+__device__ __forceinline__ int64_t node_addr(int64_t block_begin, int nb, int ix, int iy, int iz) {
+    int64_t blk = block_begin + ((int64_t)((ix >> 2) * nb + (iy >> 2)) * nb + (iz >> 2));
+    return blk * kBlockNodes + (((ix & 3) << 4) | ((iy & 3) << 2) | (iz & 3));
+}
+
+// scene owning a global grid block / a user-order particle (binary search)
+__device__ __forceinline__ int scene_of_block(const MpmScene *sc, int n_scenes, int64_t blk) {
+    int lo = 0, hi = n_scenes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (sc[mid].block_begin <= blk) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int scene_of_particle(const MpmScene *sc, int n_scenes, int64_t p) {
+    int lo = 0, hi = n_scenes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (sc[mid].particle_begin <= p) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// block key of a particle position: global block id or the sentinel (nbk-1)
+__device__ __forceinline__ int particle_key(const MpmScene &S, float x0x, float x0y, float x0z,
+                                            float ux, float uy, float uz, int sentinel, bool &ok) {
+    int bx, by, bz;
+    bool a = stencil_base(grid_coord(x0x, ux, S.inv_dx), S.n_grid, bx);
+    bool b = stencil_base(grid_coord(x0y, uy, S.inv_dx), S.n_grid, by);
+    bool c = stencil_base(grid_coord(x0z, uz, S.inv_dx), S.n_grid, bz);
+    ok = a && b && c;
+    const int nb = S.n_blocks_axis;
+    return ok ? (int)(S.block_begin + ((int64_t)((bx >> 2) * nb + (by >> 2)) * nb + (bz >> 2)))
+              : sentinel;
+}
+
+// warp-aggregated atomicAdd of 1 per lane into counts[key] (key < 0: skip)
+__device__ __forceinline__ void warp_histogram(int *counts, int key) {
+    unsigned peers = __match_any_sync(0xffffffffu, key);
+    int leader = __ffs(peers) - 1;
+    if (key >= 0 && (threadIdx.x & 31) == leader) atomicAdd(counts + key, __popc(peers));
+}
+
+// ---------------------------------------------------------------------------
+// 3x3 SVD: Jacobi eigen-analysis of A^T A with approximate Givens rotations
+// accumulated as a quaternion, sort by column norm, Givens QR (McAdams,
+// Selle, Tamstorf, Teran, Sifakis 2011, UW-Madison CS TR1690), the method
+// behind Warp's wp.svd3 (called at engine_stress/mpm_utils.py:64, 92, 297).
+// U, V are rotations; |s| descending; sign(det A) on s[2].
+// ---------------------------------------------------------------------------
+struct Svd {
+    float U[9], s[3], V[9];
+};
+
+// Conjugate the (p,q) block [[a,b],[b,d]] (with cross terms xp=S[p][k],
+// xq=S[q][k]) by the approximate Jacobi rotation; returns its half angle.
+__device__ __forceinline__ void jacobi_pair(float &a, float &d, float &b, float &xp, float &xq,
+                                            float &ch, float &sh) {
+    const float kGamma = 5.828427124746190f;  // 3 + 2 sqrt(2)
+    const float kCstar = 0.923879532511287f;  // cos(pi/8)
+    const float kSstar = 0.382683432365090f;  // sin(pi/8)
+    float c0 = 2.0f * (a - d), s0 = b;
+    bool small = kGamma * s0 * s0 < c0 * c0;
+    float w = rsqrtf(c0 * c0 + s0 * s0);
+    ch = small ? w * c0 : kCstar;
+    sh = small ? w * s0 : kSstar;
+    float c = ch * ch - sh * sh, s = 2.0f * ch * sh;
+    float cc = c * c, ss = s * s, cs = c * s;
+    float na = cc * a + 2.0f * cs * b + ss * d;
+    float nd = ss * a - 2.0f * cs * b + cc * d;
+    float nb = b * (cc - ss) + (d - a) * cs;
+    float np = c * xp + s * xq;
+    float nq = -s * xp + c * xq;
+    a = na; d = nd; b = nb; xp = np; xq = nq;
+}
+
+__device__ __forceinline__ void cond_swap_neg(bool sw, float B[9], float V[9], int i, int j) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        float bi = B[r * 3 + i], bj = B[r * 3 + j];
+        B[r * 3 + i] = sw ? bj : bi;
+        B[r * 3 + j] = sw ? -bi : bj;
+        float vi = V[r * 3 + i], vj = V[r * 3 + j];
+        V[r * 3 + i] = sw ? vj : vi;
+        V[r * 3 + j] = sw ? -vi : vj;
+    }
+}
+
+__device__ __forceinline__ void qr_givens(float B[9], float U[9], int p, int q, int col) {
+    float a1 = B[p * 3 + col], a2 = B[q * 3 + col];
+    float r2 = a1 * a1 + a2 * a2;
+    float ri = rsqrtf(r2);
+    bool nz = r2 > 0.0f;
+    float c = nz ? a1 * ri : 1.0f;
+    float s = nz ? a2 * ri : 0.0f;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        float bp = B[p * 3 + j], bq = B[q * 3 + j];
+        B[p * 3 + j] = c * bp + s * bq;
+        B[q * 3 + j] = -s * bp + c * bq;
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        float up = U[r * 3 + p], uq = U[r * 3 + q];
+        U[r * 3 + p] = c * up + s * uq;
+        U[r * 3 + q] = -s * up + c * uq;
+    }
+}
+
+__device__ __forceinline__ void svd3(const float A[9], Svd &out) {
+    // S = A^T A (symmetric)
+    float s00 = A[0] * A[0] + A[3] * A[3] + A[6] * A[6];
+    float s01 = A[0] * A[1] + A[3] * A[4] + A[6] * A[7];
+    float s02 = A[0] * A[2] + A[3] * A[5] + A[6] * A[8];
+    float s11 = A[1] * A[1] + A[4] * A[4] + A[7] * A[7];
+    float s12 = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
+    float s22 = A[2] * A[2] + A[5] * A[5] + A[8] * A[8];
+    float qw = 1.f, qx = 0.f, qy = 0.f, qz = 0.f;
+#pragma unroll
+    for (int sweep = 0; sweep < kSvdSweeps; ++sweep) {
+        float ch, sh, w, x, y, z;
+        // plane (0,1), axis z
+        jacobi_pair(s00, s11, s01, s02, s12, ch, sh);
+        w = qw * ch - qz * sh; x = ch * qx + qy * sh; y = ch * qy - qx * sh; z = qw * sh + ch * qz;
+        qw = w; qx = x; qy = y; qz = z;
+        // plane (1,2), axis x
+        jacobi_pair(s11, s22, s12, s01, s02, ch, sh);
+        w = qw * ch - qx * sh; x = qw * sh + ch * qx; y = ch * qy + qz * sh; z = ch * qz - qy * sh;
+        qw = w; qx = x; qy = y; qz = z;
+        // plane (2,0), axis y
+        jacobi_pair(s22, s00, s02, s12, s01, ch, sh);
+        w = qw * ch - qy * sh; x = ch * qx - qz * sh; y = qw * sh + ch * qy; z = ch * qz + qx * sh;
+        qw = w; qx = x; qy = y; qz = z;
+    }
+    float qn = rsqrtf(qw * qw + qx * qx + qy * qy + qz * qz);
+    qw *= qn; qx *= qn; qy *= qn; qz *= qn;
+    float *V = out.V;
+    V[0] = 1.f - 2.f * (qy * qy + qz * qz); V[1] = 2.f * (qx * qy - qw * qz); V[2] = 2.f * (qx * qz + qw * qy);
+    V[3] = 2.f * (qx * qy + qw * qz); V[4] = 1.f - 2.f * (qx * qx + qz * qz); V[5] = 2.f * (qy * qz - qw * qx);
+    V[6] = 2.f * (qx * qz - qw * qy); V[7] = 2.f * (qy * qz + qw * qx); V[8] = 1.f - 2.f * (qx * qx + qy * qy);
+    float B[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            B[r * 3 + c] = A[r * 3 + 0] * V[0 * 3 + c] + A[r * 3 + 1] * V[1 * 3 + c] + A[r * 3 + 2] * V[2 * 3 + c];
+    float r0 = B[0] * B[0] + B[3] * B[3] + B[6] * B[6];
+    float r1 = B[1] * B[1] + B[4] * B[4] + B[7] * B[7];
+    float r2 = B[2] * B[2] + B[5] * B[5] + B[8] * B[8];
+    bool sw = r0 < r1;
+    cond_swap_neg(sw, B, V, 0, 1);
+    { float t = r0; r0 = sw ? r1 : r0; r1 = sw ? t : r1; }
+    sw = r0 < r2;
+    cond_swap_neg(sw, B, V, 0, 2);
+    { float t = r0; r0 = sw ? r2 : r0; r2 = sw ? t : r2; }
+    sw = r1 < r2;
+    cond_swap_neg(sw, B, V, 1, 2);
+    float *U = out.U;
+    U[0] = 1.f; U[1] = 0.f; U[2] = 0.f; U[3] = 0.f; U[4] = 1.f; U[5] = 0.f; U[6] = 0.f; U[7] = 0.f; U[8] = 1.f;
+    qr_givens(B, U, 0, 1, 0);
+    qr_givens(B, U, 0, 2, 0);
+    qr_givens(B, U, 1, 2, 1);
+    out.s[0] = B[0];
+    out.s[1] = B[4];
+    out.s[2] = B[8];
+}
+
+// U diag(d) W^T
+__device__ __forceinline__ void udwt(const float U[9], const float d[3], const float W[9], float out[9]) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            out[r * 3 + c] = U[r * 3 + 0] * d[0] * W[c * 3 + 0] + U[r * 3 + 1] * d[1] * W[c * 3 + 1] +
+                             U[r * 3 + 2] * d[2] * W[c * 3 + 2];
+}
+
+// ---------------------------------------------------------------------------
+// Return mapping + Kirchhoff stress for one particle, fused on ONE SVD.
+// The reference (g2p_apic_and_stress, engine_stress/mpm_utils.py:284-306)
+// takes a second SVD of the returned F for the stress.  The returned F is
+// either F_trial itself (whose SVD is the first one, exactly) or
+// U diag(s_new) V^T, whose SVD is (U, s_new, V); so the first factors are
+// reused, and  U diag(c) V^T F^T = U diag(c * s_new) U^T  for the
+// Drucker-Prager stress (:45-52).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void return_map_stress(const MpmScene &S, const float Ft[9], float &yld,
+                                                  float Fo[9], float tau[9]) {
+    Svd d;
+    svd3(Ft, d);
+    const float mu = S.mu, lam = S.lam;
+    if (S.material == MPM_SAND) {
+        // sand_return_mapping, mpm_utils.py:87-112
+        float e0 = logf(fmaxf(fabsf(d.s[0]), 1e-14f));
+        float e1 = logf(fmaxf(fabsf(d.s[1]), 1e-14f));
+        float e2 = logf(fmaxf(fabsf(d.s[2]), 1e-14f));
+        float tr = e0 + e1 + e2;
+        float h0 = e0 - tr / 3.0f, h1 = e1 - tr / 3.0f, h2 = e2 - tr / 3.0f;
+        float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2);
+        float dg = hn + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * S.alpha;
+        float sn[3];
+        if (dg <= 0.0f) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Fo[i] = Ft[i];
+            sn[0] = d.s[0]; sn[1] = d.s[1]; sn[2] = d.s[2];
+        } else if (tr > 0.0f) {
+            sn[0] = sn[1] = sn[2] = 1.0f;
+            udwt(d.U, sn, d.V, Fo);
+        } else {
+            float r = dg / hn;
+            sn[0] = expf(e0 - h0 * r);
+            sn[1] = expf(e1 - h1 * r);
+            sn[2] = expf(e2 - h2 * r);
+            udwt(d.U, sn, d.V, Fo);
+        }
+        // kirchoff_stress_drucker_prager, mpm_utils.py:45-52 (unclamped log)
+        float l0 = logf(sn[0]), l1 = logf(sn[1]), l2 = logf(sn[2]);
+        float ls = l0 + l1 + l2;
+        float t[3] = {2.0f * mu * l0 + lam * ls, 2.0f * mu * l1 + lam * ls, 2.0f * mu * l2 + lam * ls};
+        udwt(d.U, t, d.U, tau);
+    } else if (S.material == MPM_METAL) {
+        // von_mises_return_mapping, mpm_utils.py:59-84
+        float c0 = fmaxf(d.s[0], 0.01f), c1 = fmaxf(d.s[1], 0.01f), c2 = fmaxf(d.s[2], 0.01f);
+        float e0 = logf(c0), e1 = logf(c1), e2 = logf(c2);
+        float es = e0 + e1 + e2;
+        float temp = es / 3.0f;
+        float t0 = 2.0f * mu * e0 + lam * es, t1 = 2.0f * mu * e1 + lam * es, t2 = 2.0f * mu * e2 + lam * es;
+        float st = t0 + t1 + t2;
+        float k0 = t0 - st / 3.0f, k1 = t1 - st / 3.0f, k2 = t2 - st / 3.0f;
+        float sn[3];
+        if (sqrtf(k0 * k0 + k1 * k1 + k2 * k2) > yld) {
+            float h0 = e0 - temp, h1 = e1 - temp, h2 = e2 - temp;
+            float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2) + 1e-6f;
+            float dg = hn - yld / (2.0f * mu);
+            float r = dg / hn;
+            sn[0] = expf(e0 - r * h0);
+            sn[1] = expf(e1 - r * h1);
+            sn[2] = expf(e2 - r * h2);
+            udwt(d.U, sn, d.V, Fo);
+            if (S.hardening == 1) yld = yld + 2.0f * mu * S.xi * dg;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Fo[i] = Ft[i];
+            sn[0] = d.s[0]; sn[1] = d.s[1]; sn[2] = d.s[2];
+        }
+        // kirchoff_stress_StVK, mpm_utils.py:36-43: U diag(2 mu eps + lam tr eps) V^T
+        float l0 = logf(fmaxf(sn[0], 0.01f)), l1 = logf(fmaxf(sn[1], 0.01f)), l2 = logf(fmaxf(sn[2], 0.01f));
+        float ls = l0 + l1 + l2;
+        float t[3] = {2.0f * mu * l0 + lam * ls, 2.0f * mu * l1 + lam * ls, 2.0f * mu * l2 + lam * ls};
+        udwt(d.U, t, d.V, tau);
+    } else {
+        // jelly: F = F_trial, kirchoff_stress_FCR (mpm_utils.py:29-34)
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Fo[i] = Ft[i];
+        float J = Ft[0] * (Ft[4] * Ft[8] - Ft[5] * Ft[7]) - Ft[1] * (Ft[3] * Ft[8] - Ft[5] * Ft[6]) +
+                  Ft[2] * (Ft[3] * Ft[7] - Ft[4] * Ft[6]);
+        float one[3] = {1.f, 1.f, 1.f};
+        float R[9];
+        udwt(d.U, one, d.V, R);
+        float D[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) D[i] = 2.0f * mu * (Ft[i] - R[i]);
+        float dia = lam * J * (J - 1.0f);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                tau[r * 3 + c] = D[r * 3 + 0] * Ft[c * 3 + 0] + D[r * 3 + 1] * Ft[c * 3 + 1] +
+                                 D[r * 3 + 2] * Ft[c * 3 + 2] + (r == c ? dia : 0.0f);
+    }
+}
+
+}  // namespace mpm

@@ -1,0 +1,184 @@
+// Data movement between the reference layout (AoS, user particle order) and
+// the internal sorted SoA state, the dense grid export, and the batched
+// element kernels (SVD, return map) used for unit-level checks.
+#include "mpm_device.cuh"
+#include "mpm_launch.h"
+
+namespace mpm {
+
+int field_components(int field) {
+    switch (field) {
+        case MPM_FIELD_X_INITIAL: case MPM_FIELD_U: case MPM_FIELD_V: case MPM_FIELD_X: return 3;
+        case MPM_FIELD_C: case MPM_FIELD_F: case MPM_FIELD_STRESS: case MPM_FIELD_F_DISP: return 9;
+        case MPM_FIELD_MASS: case MPM_FIELD_VOL: case MPM_FIELD_YIELD: return 1;
+        default: return 0;
+    }
+}
+
+__device__ __forceinline__ float *field_ptr(const PState &st, int field) {
+    switch (field) {
+        case MPM_FIELD_X_INITIAL: return st.x0;
+        case MPM_FIELD_U: return st.u;
+        case MPM_FIELD_V: return st.v;
+        case MPM_FIELD_C: return st.C;
+        case MPM_FIELD_F: case MPM_FIELD_F_DISP: return st.F;
+        case MPM_FIELD_STRESS: return st.tau;
+        case MPM_FIELD_MASS: return st.mass;
+        case MPM_FIELD_VOL: return st.vol;
+        case MPM_FIELD_YIELD: return st.yld;
+        default: return st.u;  // MPM_FIELD_X reads u (plus x0)
+    }
+}
+
+// initial values of MPM_Simulator_WARP.initialize (mpm_solver_warp.py:52-69):
+// zero everything, F = I (as load_from_sampling leaves it, :149), slot = user index
+__global__ void init_state_kernel(PState a, PState b, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t s = a.stride;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        float v = (k % 4 == 0) ? 1.0f : 0.0f;
+        a.F[i + k * s] = v;
+        b.F[i + k * s] = v;
+    }
+    a.uid[i] = i;
+    b.uid[i] = i;
+    a.key[i] = -1;
+    b.key[i] = -1;
+}
+
+__global__ void load_kernel(PState st, int n, int field, int nc, const float *__restrict__ src) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t u = st.uid[i];
+    float *dst = field_ptr(st, field);
+    for (int c = 0; c < nc; ++c) dst[i + c * st.stride] = src[u * nc + c];
+}
+
+__global__ void export_kernel(PState st, int n, int field, int nc, float *__restrict__ dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t u = st.uid[i];
+    const float *src = field_ptr(st, field);
+    for (int c = 0; c < nc; ++c) {
+        float v = src[i + c * st.stride];
+        if (field == MPM_FIELD_X) v = __fadd_rn(st.x0[i + c * st.stride], v);       // x0 + u (:5-7)
+        if (field == MPM_FIELD_F_DISP) v = v - ((c % 4 == 0) ? 1.0f : 0.0f);       // F - I (:16-19)
+        dst[u * nc + c] = v;
+    }
+}
+
+// dense (n,n,n) grid_m / grid_v_in from the accumulator (valid after p2g)
+__global__ void export_acc_kernel(const float4 *__restrict__ acc, int64_t block_begin, int nb, int n,
+                                  float *gm, float *gvin) {
+    int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t nn = (int64_t)n * n * n;
+    if (g >= nn) return;
+    int iz = (int)(g % n), iy = (int)((g / n) % n), ix = (int)(g / ((int64_t)n * n));
+    float4 a = acc[node_addr(block_begin, nb, ix, iy, iz)];
+    if (gm) gm[g] = a.w;
+    if (gvin) { gvin[3 * g] = a.x; gvin[3 * g + 1] = a.y; gvin[3 * g + 2] = a.z; }
+}
+
+// grid_v_out of the active blocks that belong to one scene (rest stays 0)
+__global__ void export_vout_kernel(const float4 *__restrict__ gridv, const int *__restrict__ list,
+                                   const int *__restrict__ n_active, MpmScene S, float *gvout) {
+    const int na = *n_active;
+    const int nb = S.n_blocks_axis, n = S.n_grid;
+    const int64_t nblk = (int64_t)nb * nb * nb;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (int64_t)na * kBlockNodes;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        int gb = list[j >> 6];
+        int64_t lb = gb - S.block_begin;
+        if (lb < 0 || lb >= nblk) continue;
+        int l = (int)(j & 63);
+        int bz = (int)(lb % nb), by = (int)((lb / nb) % nb), bx = (int)(lb / ((int64_t)nb * nb));
+        int ix = 4 * bx + (l >> 4), iy = 4 * by + ((l >> 2) & 3), iz = 4 * bz + (l & 3);
+        if (ix >= n || iy >= n || iz >= n) continue;
+        float4 v = gridv[(int64_t)gb * kBlockNodes + l];
+        int64_t g = ((int64_t)ix * n + iy) * n + iz;
+        gvout[3 * g] = v.x; gvout[3 * g + 1] = v.y; gvout[3 * g + 2] = v.z;
+    }
+}
+
+__global__ void svd_kernel(const float *__restrict__ A, float *U, float *s, float *V, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float a[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) a[k] = A[9 * i + k];
+    Svd d;
+    svd3(a, d);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { U[9 * i + k] = d.U[k]; V[9 * i + k] = d.V[k]; }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) s[3 * i + k] = d.s[k];
+}
+
+__global__ void return_map_kernel(MpmScene S, const float *__restrict__ Ft, float *yld, float *F,
+                                  float *tau, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float a[9], fo[9], t[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) a[k] = Ft[9 * i + k];
+    float y = yld ? yld[i] : 0.0f;
+    return_map_stress(S, a, y, fo, t);
+    if (yld) yld[i] = y;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { F[9 * i + k] = fo[k]; tau[9 * i + k] = t[k]; }
+}
+
+static inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+cudaError_t launch_init_state(const Ctx &cx, const PState &other) {
+    if (cx.n == 0) return cudaSuccess;
+    init_state_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, other, cx.n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_load(const Ctx &cx, int field, const float *src) {
+    if (cx.n == 0) return cudaSuccess;
+    load_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, field,
+                                                               field_components(field), src);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export(const Ctx &cx, int field, float *dst) {
+    if (cx.n == 0) return cudaSuccess;
+    export_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, field,
+                                                                 field_components(field), dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_grid(const Ctx &cx, const MpmScene &S, int scene_index, float *gm,
+                               float *gvin, float *gvout) {
+    (void)scene_index;
+    const int64_t nn = (int64_t)S.n_grid * S.n_grid * S.n_grid;
+    if (gm || gvin)
+        export_acc_kernel<<<blocks_for(nn, 256), 256, 0, cx.stream>>>(
+            cx.ws.grid_acc, S.block_begin, S.n_blocks_axis, S.n_grid, gm, gvin);
+    if (gvout) {
+        cudaError_t e = cudaMemsetAsync(gvout, 0, (size_t)nn * 3 * sizeof(float), cx.stream);
+        if (e != cudaSuccess) return e;
+        export_vout_kernel<<<cx.num_sms * 4, 256, 0, cx.stream>>>(cx.ws.grid_v, cx.ws.active_list,
+                                                                   cx.ws.n_active, S, gvout);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_svd3(const float *A, float *U, float *s, float *V, int64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    svd_kernel<<<blocks_for(n, 128), 128, 0, st>>>(A, U, s, V, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_return_map(const MpmScene &scene, const float *Ft, float *yld, float *F,
+                              float *tau, int64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    return_map_kernel<<<blocks_for(n, 128), 128, 0, st>>>(scene, Ft, yld, F, tau, n);
+    return cudaGetLastError();
+}
+
+}  // namespace mpm

@@ -1,0 +1,45 @@
+// Internal launch interface between the C-ABI layer (mpm_api.cu) and the
+// kernel translation units.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mpm_device.cuh"
+
+namespace mpm {
+
+struct Ctx {
+    const MpmScene *scenes;  // device scene table
+    int n_scenes;
+    PState st;               // live state buffer
+    Ws ws;
+    int n;                   // particles
+    int *status;
+    cudaStream_t stream;
+    int num_sms;
+    int64_t total_blocks;
+};
+
+// sort stage (mpm_sort.cu)
+cudaError_t launch_keys(const Ctx &cx);
+cudaError_t launch_sort(const Ctx &cx);
+cudaError_t launch_permute(const Ctx &cx, const PState &dst);
+
+// transfer stages (mpm_substep.cu)
+cudaError_t launch_p2g(const Ctx &cx, float dt);
+cudaError_t launch_grid(const Ctx &cx, float time, float dt);
+cudaError_t launch_g2p(const Ctx &cx, float dt);
+
+// data movement and element kernels (mpm_io.cu)
+cudaError_t launch_init_state(const Ctx &cx, const PState &other);
+cudaError_t launch_load(const Ctx &cx, int field, const float *src);
+cudaError_t launch_export(const Ctx &cx, int field, float *dst);
+cudaError_t launch_export_grid(const Ctx &cx, const MpmScene &host_scene, int scene_index,
+                               float *gm, float *gvin, float *gvout);
+cudaError_t launch_svd3(const float *A, float *U, float *s, float *V, int64_t n, cudaStream_t st);
+cudaError_t launch_return_map(const MpmScene &scene, const float *Ft, float *yld, float *F,
+                              float *tau, int64_t n, cudaStream_t st);
+
+int field_components(int field);
+
+}  // namespace mpm

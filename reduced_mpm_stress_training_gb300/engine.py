@@ -1,0 +1,318 @@
+"""Host side of the GB300 substep: buffers, scene table, stages, status.
+
+``MPMEngine`` owns the device memory (PyTorch tensors) of one or many scenes
+and drives libmpm_gb300.so through its C ABI on the current PyTorch CUDA
+stream.  The single-scene drop-in ``MPM_Simulator_WARP`` (solver.py) and
+the batched multi-scene runner (batched.py) are both thin layers over it.
+
+Particle data crosses this boundary only in the reference's layout -- AoS,
+user particle order, vec3 = 3 floats, mat33 = 9 floats row-major
+(engine_stress/warp_utils.py:5-43) -- and lives on the device in the
+library's sorted structure-of-arrays layout in between.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+import warnings
+
+import torch
+
+from . import _capi as A
+
+_MATERIALS = {"jelly": A.JELLY, "metal": A.METAL, "sand": A.SAND}
+
+
+class MPMStatusError(RuntimeError):
+    """The device status word reported a physics fault (see ``status_text``)."""
+
+    def __init__(self, bits: int):
+        self.bits = bits
+        super().__init__(f"MPM status 0x{bits:x}: {A.status_text(bits)}")
+
+
+def material_code(material) -> int:
+    """engine_stress/mpm_solver_warp.py:90-94 (TypeError on an unknown name)."""
+    if isinstance(material, int) and material in (0, 1, 2):
+        return material
+    if material not in _MATERIALS:
+        raise TypeError("Undefined material type")
+    return _MATERIALS[material]
+
+
+def lame_from_E_nu(E: float, nu: float) -> tuple[float, float]:
+    """engine_stress/mpm_solver_warp.py:41-42"""
+    return E / 2.0 / (1.0 + nu), E * nu / (1.0 + nu) / (1.0 - 2.0 * nu)
+
+
+def dp_alpha(friction_angle: float) -> float:
+    """Drucker-Prager alpha, engine_stress/mpm_solver_warp.py:113-116."""
+    sin_phi = math.sin(friction_angle / 180.0 * 3.14159265)
+    return math.sqrt(2.0 / 3.0) * 2.0 * sin_phi / (3.0 - sin_phi)
+
+
+@dataclasses.dataclass
+class Collider:
+    """Dirichlet_collider subset (engine_stress/warp_utils.py:126-151)."""
+    kind: int
+    point: tuple = (0.0, 0.0, 0.0)
+    normal: tuple = (0.0, 0.0, 1.0)
+    surface_type: int = 0
+    friction: float = 0.0
+    start_time: float = 0.0
+    end_time: float = 999.0
+
+    @staticmethod
+    def surface(point, normal, surface="sticky", friction=0.0, start_time=0.0, end_time=999.0):
+        """engine_stress/mpm_solver_warp.py:407-428 (normal normalised, sticky needs friction 0)."""
+        point = list(point)
+        scale = 1.0 / math.sqrt(sum(x ** 2 for x in normal))
+        normal = [scale * x for x in normal]
+        if surface == "sticky" and friction != 0:
+            raise ValueError("friction must be 0 on sticky surfaces.")
+        st = 0 if surface == "sticky" else (1 if surface == "slip" else 2)
+        return Collider(A.COLLIDER_SURFACE, tuple(point), tuple(normal), st, friction,
+                        start_time, end_time)
+
+    @staticmethod
+    def bounding_box(start_time=0.0, end_time=999.0):
+        """engine_stress/mpm_solver_warp.py:499-503"""
+        return Collider(A.COLLIDER_BOX, start_time=start_time, end_time=end_time)
+
+    def to_struct(self) -> A.MpmCollider:
+        c = A.MpmCollider()
+        c.kind = self.kind
+        c.surface_type = self.surface_type
+        for i in range(3):
+            c.point[i] = self.point[i]
+            c.normal[i] = self.normal[i]
+        c.friction = self.friction
+        c.start_time = self.start_time
+        c.end_time = self.end_time
+        return c
+
+
+@dataclasses.dataclass
+class SceneParams:
+    """MPMModelStruct (engine_stress/warp_utils.py:61-81) of one scene."""
+    n_particles: int
+    n_grid: int = 100
+    grid_lim: float = 1.0
+    material: int = A.JELLY
+    mu: float = 1000 / 2.0 / 1.3           # E=1000, nu=0.3 defaults (:39-42)
+    lam: float = 1000 * 0.3 / 1.3 / 0.4
+    friction_angle: float = 25.0           # (:46-48)
+    hardening: int = 0
+    xi: float = 0.0
+    gravity: tuple = (0.0, 0.0, 0.0)       # reference default g = 0 (:49)
+    colliders: list = dataclasses.field(default_factory=list)
+
+    @property
+    def dx(self) -> float:
+        return self.grid_lim / self.n_grid
+
+    @property
+    def inv_dx(self) -> float:
+        return float(self.n_grid / self.grid_lim)
+
+    def to_struct(self, particle_begin: int) -> A.MpmScene:
+        s = A.MpmScene()
+        s.n_grid = self.n_grid
+        s.material = self.material
+        s.hardening = int(self.hardening)
+        if len(self.colliders) > A.MPM_MAX_COLLIDERS:
+            raise ValueError(f"at most {A.MPM_MAX_COLLIDERS} colliders per scene")
+        s.n_colliders = len(self.colliders)
+        s.dx = self.dx
+        s.inv_dx = self.inv_dx
+        s.mu = self.mu
+        s.lam = self.lam
+        s.alpha = dp_alpha(self.friction_angle)
+        s.xi = self.xi
+        for i in range(3):
+            s.gravity[i] = self.gravity[i]
+        s.particle_begin = particle_begin
+        s.particle_count = self.n_particles
+        for k, c in enumerate(self.colliders):
+            s.colliders[k] = c.to_struct()
+        return s
+
+
+def _stream_handle(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+class MPMEngine:
+    """Device buffers + C-ABI driver for one or more scenes (concatenated)."""
+
+    def __init__(self, scenes: list[SceneParams], device="cuda:0", chunk_size: int = 128,
+                 resort_interval: int = 16):
+        self.lib = A.load()
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError("MPMEngine runs on a CUDA device only (no CPU path)")
+        self.scenes = list(scenes)
+        self.chunk_size = chunk_size
+        self.resort_interval = resort_interval
+        self.on_error = "raise"
+        self._pending = None
+        self._allocate(fresh=True)
+
+    # ------------------------------------------------------------------ layout
+    @property
+    def n_particles(self) -> int:
+        return sum(s.n_particles for s in self.scenes)
+
+    def _scene_table(self):
+        arr = (A.MpmScene * len(self.scenes))()
+        begin = 0
+        for i, s in enumerate(self.scenes):
+            arr[i] = s.to_struct(begin)
+            begin += s.n_particles
+        return arr
+
+    def _allocate(self, fresh: bool) -> None:
+        """Plan and allocate; fresh=False keeps the particle state (grid change)."""
+        table = self._scene_table()
+        plan = A.MpmPlan()
+        A.check(self.lib.mpm_plan(table, len(self.scenes), self.n_particles, self.chunk_size,
+                                  C.byref(plan)), "mpm_plan")
+        self.table = table
+        self.plan = plan
+        dev = self.device
+        with torch.cuda.device(dev):
+            if fresh:
+                self._state = [torch.empty(plan.state_bytes, dtype=torch.uint8, device=dev)
+                               for _ in range(2)]
+                self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+                self._status_host = torch.zeros(1, dtype=torch.int32).pin_memory()
+                self._status_event = torch.cuda.Event()
+            self._workspace = torch.zeros(plan.workspace_bytes, dtype=torch.uint8, device=dev)
+            self._scenes_dev = torch.empty(C.sizeof(A.MpmScene) * len(self.scenes),
+                                           dtype=torch.uint8, device=dev)
+        b = A.MpmBuffers() if fresh else self.buf
+        b.state[0] = self._state[0].data_ptr()
+        b.state[1] = self._state[1].data_ptr()
+        b.workspace = self._workspace.data_ptr()
+        b.scenes = self._scenes_dev.data_ptr()
+        b.status = self._status.data_ptr()
+        b.plan = plan
+        b.resort_interval = self.resort_interval
+        self.buf = b
+        self._upload()
+        if fresh:
+            A.check(self.lib.mpm_init(C.byref(b), self.stream), "mpm_init")
+        else:
+            b.keys_valid = 0  # block keys depend on the grid
+
+    def _upload(self) -> None:
+        table = self._scene_table()
+        A.check(self.lib.mpm_plan(table, len(self.scenes), self.n_particles, self.chunk_size,
+                                  C.byref(A.MpmPlan())), "mpm_plan")
+        self.table = table
+        A.check(self.lib.mpm_upload_scenes(C.byref(self.buf), table, len(self.scenes),
+                                           self.stream), "mpm_upload_scenes")
+
+    def update_scenes(self, regrid: bool = False) -> None:
+        """Push changed scene parameters; regrid=True when n_grid/grid_lim changed."""
+        if regrid:
+            self._allocate(fresh=False)
+        else:
+            self._upload()
+
+    @property
+    def stream(self) -> int:
+        return _stream_handle(self.device)
+
+    # ------------------------------------------------------------------ data
+    def _as_input(self, t, comps: int) -> torch.Tensor:
+        t = torch.as_tensor(t)
+        n = self.n_particles
+        if t.numel() != n * comps:
+            raise ValueError(f"expected {n} x {comps} values, got shape {tuple(t.shape)}")
+        return t.detach().to(device=self.device, dtype=torch.float32).reshape(n * comps).contiguous()
+
+    def load(self, field: int, t) -> None:
+        src = self._as_input(t, A.FIELD_COMPONENTS[field])
+        # src is stream-ordered on the current stream, so the caching
+        # allocator cannot hand its memory out before the load kernel ran
+        A.check(self.lib.mpm_load(C.byref(self.buf), field, src.data_ptr(), 0, self.stream),
+                "mpm_load")
+
+    def load_host(self, field: int, host: torch.Tensor) -> None:
+        """Load from a (pinned) host tensor through the library's staging copy."""
+        assert host.device.type == "cpu" and host.dtype == torch.float32 and host.is_contiguous()
+        A.check(self.lib.mpm_load(C.byref(self.buf), field, host.data_ptr(), 1, self.stream),
+                "mpm_load")
+
+    def export(self, field: int, out: torch.Tensor | None = None) -> torch.Tensor:
+        comps = A.FIELD_COMPONENTS[field]
+        n = self.n_particles
+        if out is None:
+            out = torch.empty(n * comps, dtype=torch.float32, device=self.device)
+        on_host = out.device.type == "cpu"
+        A.check(self.lib.mpm_export(C.byref(self.buf), field, out.data_ptr(), int(on_host),
+                                    self.stream), "mpm_export")
+        return out
+
+    def export_grid(self, scene: int = 0):
+        ng = self.scenes[scene].n_grid
+        gm = torch.empty((ng, ng, ng), dtype=torch.float32, device=self.device)
+        gvin = torch.empty((ng, ng, ng, 3), dtype=torch.float32, device=self.device)
+        gvout = torch.empty((ng, ng, ng, 3), dtype=torch.float32, device=self.device)
+        A.check(self.lib.mpm_export_grid(C.byref(self.buf), scene, gm.data_ptr(), gvin.data_ptr(),
+                                         gvout.data_ptr(), self.stream), "mpm_export_grid")
+        return gm, gvin, gvout
+
+    # ------------------------------------------------------------------ stepping
+    def substep(self, time: float, dt: float) -> None:
+        self.poll_status()
+        A.check(self.lib.mpm_p2g2p(C.byref(self.buf), time, dt, self.stream), "mpm_p2g2p")
+        self._queue_status()
+
+    def stage(self, name: str, time: float = 0.0, dt: float = 0.0) -> None:
+        b = C.byref(self.buf)
+        s = self.stream
+        if name == "sort":
+            A.check(self.lib.mpm_sort(b, s), "mpm_sort")
+        elif name == "p2g":
+            A.check(self.lib.mpm_p2g(b, dt, s), "mpm_p2g")
+        elif name == "grid":
+            A.check(self.lib.mpm_grid_update(b, time, dt, s), "mpm_grid_update")
+        elif name == "g2p":
+            A.check(self.lib.mpm_g2p(b, dt, s), "mpm_g2p")
+        else:
+            raise ValueError(name)
+
+    # ------------------------------------------------------------------ status
+    def _queue_status(self) -> None:
+        self._status_host.copy_(self._status, non_blocking=True)
+        self._status_event.record(torch.cuda.current_stream(self.device))
+        self._pending = True
+
+    def poll_status(self, wait: bool = False) -> int:
+        """Read the status word copied after the last substep (lazy; no sync
+        unless wait=True) and act on it per ``on_error``."""
+        if not self._pending:
+            return 0
+        if not wait and not self._status_event.query():
+            return 0
+        self._status_event.synchronize()
+        self._pending = False
+        bits = int(self._status_host.item())
+        if bits:
+            self._status.zero_()
+            if self.on_error == "raise":
+                raise MPMStatusError(bits)
+            if self.on_error == "warn":
+                warnings.warn(str(MPMStatusError(bits)))
+        return bits
+
+    def status(self) -> int:
+        """Synchronously read (without clearing) the device status word."""
+        return int(self._status.item())
+
+    def clear_status(self) -> None:
+        self._status.zero_()
+        self._pending = False

@@ -1,0 +1,274 @@
+"""Drop-in for ``MPM_Simulator_WARP`` (engine_stress/mpm_solver_warp.py:24-720).
+
+Same class name (alias), constructor, method names, keyword arguments and
+error behaviour on the substep path; the work runs in libmpm_gb300.so on
+the current PyTorch CUDA stream.  Differences a caller can see:
+
+* Device buffers are owned by this object; tensors handed to the loaders
+  are copied (``clone=False`` is accepted but never aliases), and the
+  ``export_*`` / ``mpm_state.*`` readers return fresh tensors in the user's
+  particle order (the device copy is kept sorted by grid block).
+* Errors the reference meets with ``input()`` or undefined indexing (CFL
+  violation :188-192, particles leaving the grid) set bits in a device
+  status word, read lazily after each substep; ``on_error`` decides whether
+  they raise ``MPMStatusError`` (default), warn or are ignored.  The
+  reference's per-substep debug prints (:173-190) are dropped; print_norm
+  works as before.
+* ``initialize`` starts from F = I (the reference leaves F = 0 until
+  ``load_from_sampling`` sets it to I, :149).
+* Extensions: ``set_parameters(E=, nu=, gravity=(gx,gy,gz), particle_vol=)``,
+  ``load_vol_from_tensor``, ``load_F_from_tensor``, ``load_yield_from_tensor``.
+* Colliders other than the surface collider and the bounding box raise
+  NotImplementedError.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _capi as A
+from .engine import (Collider, MPMEngine, MPMStatusError, SceneParams, lame_from_E_nu,
+                     material_code, dp_alpha)
+
+
+class _Model:
+    """Readable mirror of MPMModelStruct (engine_stress/warp_utils.py:61-81)."""
+
+    def __init__(self, sim: "MPMSimulator"):
+        self._sim = sim
+
+    def __getattr__(self, name):
+        sp = self.__dict__["_sim"]._params
+        table = {
+            "grid_lim": sp.grid_lim, "n_grid": sp.n_grid, "grid_dim_x": sp.n_grid,
+            "grid_dim_y": sp.n_grid, "grid_dim_z": sp.n_grid, "dx": sp.dx, "inv_dx": sp.inv_dx,
+            "mu": sp.mu, "lam": sp.lam, "material": sp.material, "friction_angle": sp.friction_angle,
+            "alpha": dp_alpha(sp.friction_angle), "hardening": sp.hardening, "xi": sp.xi,
+            "gravitational_accelaration": -sp.gravity[1], "gravity": sp.gravity,
+            "n_particles": sp.n_particles,
+        }
+        if name in table:
+            return table[name]
+        if name == "yield_stress":
+            return self.__dict__["_sim"]._engine.export(A.FIELD_YIELD)
+        raise AttributeError(name)
+
+
+class _State:
+    """Readers of MPMStateStruct fields (engine_stress/warp_utils.py:84-124) in user order."""
+
+    _VEC = {"particle_x": A.FIELD_X, "particle_x_initial": A.FIELD_X_INITIAL,
+            "particle_u": A.FIELD_U, "particle_v": A.FIELD_V}
+    _MAT = {"particle_F": A.FIELD_F, "particle_C": A.FIELD_C, "particle_stress": A.FIELD_STRESS}
+    _SCALAR = {"particle_mass": A.FIELD_MASS, "particle_vol": A.FIELD_VOL}
+
+    def __init__(self, sim: "MPMSimulator"):
+        self._sim = sim
+
+    def __getattr__(self, name):
+        sim = self.__dict__["_sim"]
+        eng = sim._engine
+        n = sim.n_particles
+        if name in self._VEC:
+            return eng.export(self._VEC[name]).reshape(n, 3)
+        if name in self._MAT:
+            return eng.export(self._MAT[name]).reshape(n, 3, 3)
+        if name in self._SCALAR:
+            return eng.export(self._SCALAR[name])
+        if name == "particle_F_disp":
+            return sim._f_disp()
+        if name == "particle_density":
+            return sim._density
+        if name in ("grid_m", "grid_v_in", "grid_v_out"):
+            gm, gvin, gvout = eng.export_grid(0)
+            return {"grid_m": gm, "grid_v_in": gvin, "grid_v_out": gvout}[name]
+        raise AttributeError(name)
+
+
+class MPMSimulator:
+    """GB300 replacement of MPM_Simulator_WARP (engine_stress/mpm_solver_warp.py:24)."""
+
+    def __init__(self, n_particles, n_grid=100, grid_lim=1.0, device="cuda:0", *,
+                 chunk_size: int = 128, resort_interval: int = 16):
+        self._chunk_size = chunk_size
+        self._resort_interval = resort_interval
+        self.initialize(n_particles, n_grid, grid_lim, device=device)
+
+    # --------------------------------------------------------------- set-up
+    def initialize(self, n_particles, n_grid=100, grid_lim=1.0, device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:28-87 (defaults E=1000, nu=0.3, phi=25, g=0)."""
+        self.n_particles = int(n_particles)
+        mu, lam = lame_from_E_nu(1000.0, 0.3)
+        self._params = SceneParams(n_particles=self.n_particles, n_grid=int(n_grid),
+                                   grid_lim=float(grid_lim), material=A.JELLY, mu=mu, lam=lam,
+                                   friction_angle=25.0, gravity=(0.0, 0.0, 0.0))
+        self._E, self._nu = 1000.0, 0.3
+        self._engine = MPMEngine([self._params], device=device, chunk_size=self._chunk_size,
+                                 resort_interval=self._resort_interval)
+        self.device = self._engine.device
+        self._density = torch.zeros(self.n_particles, dtype=torch.float32, device=self.device)
+        self._f_disp_loaded = None
+        self.time = 0.0
+        self.mpm_model = _Model(self)
+        self.mpm_state = _State(self)
+
+    @property
+    def on_error(self) -> str:
+        return self._engine.on_error
+
+    @on_error.setter
+    def on_error(self, v: str) -> None:
+        if v not in ("raise", "warn", "ignore"):
+            raise ValueError(v)
+        self._engine.on_error = v
+
+    def set_parameters(self, device="cuda:0", **kwargs):
+        """engine_stress/mpm_solver_warp.py:89-127, plus E/nu/gravity/particle_vol."""
+        p = self._params
+        if "material" in kwargs:
+            p.material = material_code(kwargs["material"])
+        regrid = False
+        if "grid_lim" in kwargs:
+            p.grid_lim = float(kwargs["grid_lim"])
+            regrid = True
+        if "n_grid" in kwargs:
+            p.n_grid = int(kwargs["n_grid"])
+            regrid = True
+        if "E" in kwargs or "nu" in kwargs:
+            self._E = float(kwargs.get("E", self._E))
+            self._nu = float(kwargs.get("nu", self._nu))
+            p.mu, p.lam = lame_from_E_nu(self._E, self._nu)
+        if "mu" in kwargs:
+            p.mu = float(kwargs["mu"])
+        if "lam" in kwargs:
+            p.lam = float(kwargs["lam"])
+        if "hardening" in kwargs:
+            p.hardening = int(kwargs["hardening"])
+        if "xi" in kwargs:
+            p.xi = float(kwargs["xi"])
+        if "friction_angle" in kwargs:
+            p.friction_angle = float(kwargs["friction_angle"])
+        if "g" in kwargs:
+            p.gravity = (0.0, -float(kwargs["g"]), 0.0)  # mpm_utils.py:236
+        if "gravity" in kwargs:
+            g = tuple(float(x) for x in kwargs["gravity"])
+            if len(g) != 3:
+                raise ValueError("gravity must have 3 components")
+            p.gravity = g
+        self._engine.update_scenes(regrid=regrid)
+        if "yield_stress" in kwargs:
+            self._engine.load(A.FIELD_YIELD, torch.full((self.n_particles,),
+                                                        float(kwargs["yield_stress"])))
+        if "particle_vol" in kwargs:
+            self.load_vol_from_tensor(torch.broadcast_to(
+                torch.as_tensor(kwargs["particle_vol"], dtype=torch.float32),
+                (self.n_particles,)))
+        if "density" in kwargs:
+            # set_value_to_float_array + get_float_array_product (:121-124)
+            self._density = torch.full((self.n_particles,), float(kwargs["density"]),
+                                       dtype=torch.float32, device=self.device)
+            vol = self._engine.export(A.FIELD_VOL)
+            self._engine.load(A.FIELD_MASS, self._density * vol)
+
+    # --------------------------------------------------------------- loaders
+    def load_x_initial_from_tensor(self, tensor_x_iniital, device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:229-230"""
+        self._engine.load(A.FIELD_X_INITIAL, tensor_x_iniital)
+
+    def load_mass_from_tensor(self, tensor_mass, device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:231-232"""
+        self._engine.load(A.FIELD_MASS, tensor_mass)
+
+    def load_uvF_from_tensor(self, tensor_u, tensor_v, tensor_F, clone=True, device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:234-245.  Sets u, v and F_disp; as in the
+        reference, the substep keeps reading particle_F, so F_disp only shows in
+        exports until the next substep overwrites it with F - I."""
+        self._engine.load(A.FIELD_U, tensor_u)
+        self._engine.load(A.FIELD_V, tensor_v)
+        self._f_disp_loaded = torch.as_tensor(tensor_F).detach().to(
+            self.device, torch.float32).reshape(self.n_particles, 3, 3).clone()
+
+    def load_C_from_tensor(self, tensor_C, clone=True, device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:247-251"""
+        self._engine.load(A.FIELD_C, tensor_C)
+
+    def load_uvstress_from_tensor(self, tensor_u, tensor_v, tensor_stress, clone=True,
+                                  device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:253-266 (the learned-stress hook)."""
+        self._engine.load(A.FIELD_U, tensor_u)
+        self._engine.load(A.FIELD_V, tensor_v)
+        self._engine.load(A.FIELD_STRESS, tensor_stress)
+
+    # extensions (no reference counterpart)
+    def load_vol_from_tensor(self, tensor_vol):
+        self._engine.load(A.FIELD_VOL, tensor_vol)
+
+    def load_F_from_tensor(self, tensor_F):
+        self._engine.load(A.FIELD_F, tensor_F)
+
+    def load_yield_from_tensor(self, tensor_yield):
+        self._engine.load(A.FIELD_YIELD, tensor_yield)
+
+    def load_v_from_tensor(self, tensor_v):
+        self._engine.load(A.FIELD_V, tensor_v)
+
+    # --------------------------------------------------------------- substep
+    def p2g2p(self, step, dt, print_norm=False, device="cuda:0"):
+        """One substep, engine_stress/mpm_solver_warp.py:156-203."""
+        self._engine.substep(float(self.time), float(dt))
+        self._f_disp_loaded = None
+        self.time = self.time + dt
+        if print_norm:
+            u, v, fd, st = self.export_uvFstress_from_warp()
+            print("at mpm step", step, end=" ")
+            print("norm of u, v, F_disp, stress, respectively: ",
+                  "{:.4f}".format(float(torch.linalg.norm(u))),
+                  "{:.4f}".format(float(torch.linalg.norm(v))),
+                  "{:.4f}".format(float(torch.linalg.norm(fd))),
+                  "{:.4f}".format(float(torch.linalg.norm(st))))
+
+    def check_status(self) -> int:
+        """Wait for the last substep's status word and act on it (``on_error``)."""
+        return self._engine.poll_status(wait=True)
+
+    # --------------------------------------------------------------- readers
+    def _f_disp(self) -> torch.Tensor:
+        if self._f_disp_loaded is not None:
+            return self._f_disp_loaded.clone()
+        return self._engine.export(A.FIELD_F_DISP).reshape(self.n_particles, 3, 3)
+
+    def export_uvFstress_from_warp(self, device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:305-310 -> (u, v, F_disp, stress)."""
+        n = self.n_particles
+        e = self._engine
+        return (e.export(A.FIELD_U).reshape(n, 3), e.export(A.FIELD_V).reshape(n, 3),
+                self._f_disp(), e.export(A.FIELD_STRESS).reshape(n, 3, 3))
+
+    # --------------------------------------------------------------- colliders
+    def add_surface_collider(self, point, normal, surface="sticky", friction=0.0,
+                             start_time=0.0, end_time=999.0):
+        """engine_stress/mpm_solver_warp.py:407-451"""
+        self._params.colliders.append(Collider.surface(point, normal, surface, friction,
+                                                       start_time, end_time))
+        self._engine.update_scenes()
+
+    def add_bounding_box(self, start_time=0.0, end_time=999.0):
+        """engine_stress/mpm_solver_warp.py:499-525"""
+        self._params.colliders.append(Collider.bounding_box(start_time, end_time))
+        self._engine.update_scenes()
+
+    def _not_built(self, *a, **k):
+        raise NotImplementedError("this collider is outside the GB300 substep's scope "
+                                  "(only add_surface_collider and add_bounding_box are built)")
+
+    add_surface_collider2 = _not_built
+    set_velocity_on_infinite_plane = _not_built
+    set_column_moving_as_circle = _not_built
+    set_rotation_on_disk = _not_built
+    set_velocity_on_cube = _not_built
+    add_sphere_leader = _not_built
+    p2g2p_reduced = _not_built
+
+
+MPM_Simulator_WARP = MPMSimulator
+
+__all__ = ["MPMSimulator", "MPM_Simulator_WARP", "MPMStatusError"]

@@ -1,0 +1,159 @@
+"""Generate the closed-form known-answer fixtures in this directory.
+
+The reference (zeshunzong/reduced_mpm_stress_training) ships no tests or
+golden vectors, and its Warp solver cannot run here, so these fixtures are
+analytic: each value is computed with plain ``math`` from the formulas of
+the reference, written out independently of the oracle's code.
+
+  kat_return_map.json  return mapping + Kirchhoff stress of DIAGONAL F_trial
+                       (SVD factors are signed permutations, so the result is
+                       closed-form): sand (engine_stress/mpm_utils.py:87-112,
+                       :45-52), metal (:59-84, :36-43), jelly (:29-34)
+  kat_p2g.json         one particle's P2G contributions to its 27 nodes
+                       (engine_stress/mpm_utils.py:190-227)
+
+Run:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def lame(E, nu):
+    return E / 2.0 / (1.0 + nu), E * nu / (1.0 + nu) / (1.0 - 2.0 * nu)
+
+
+def alpha(phi):
+    s = math.sin(phi / 180.0 * 3.14159265)
+    return math.sqrt(2.0 / 3.0) * 2.0 * s / (3.0 - s)
+
+
+def sand(eps, mu, lam, al):
+    tr = sum(eps)
+    eh = [e - tr / 3 for e in eps]
+    ehn = math.sqrt(sum(x * x for x in eh))
+    dg = ehn + (3 * lam + 2 * mu) / (2 * mu) * tr * al
+    if dg <= 0:
+        H, case = list(eps), "elastic"
+    elif tr > 0:
+        H, case = [0.0, 0.0, 0.0], "tension"
+    else:
+        H, case = [eps[i] - eh[i] * (dg / ehn) for i in range(3)], "shear"
+    F = [math.exp(h) for h in H]
+    ls = sum(H)
+    tau = [2 * mu * H[i] + lam * ls for i in range(3)]
+    return F, tau, case
+
+
+def metal(eps_in, mu, lam, ys):
+    sig = [max(math.exp(e), 0.01) for e in eps_in]
+    eps = [math.log(s) for s in sig]
+    es = sum(eps)
+    t = [2 * mu * e + lam * es for e in eps]
+    st = sum(t)
+    cond = math.sqrt(sum((ti - st / 3) ** 2 for ti in t))
+    if cond > ys:
+        mean = es / 3
+        eh = [e - mean for e in eps]
+        n = math.sqrt(sum(x * x for x in eh)) + 1e-6
+        dg = n - ys / (2 * mu)
+        eps2 = [eps[i] - (dg / n) * eh[i] for i in range(3)]
+        F = [math.exp(e) for e in eps2]
+        case = "plastic"
+    else:
+        F = [math.exp(e) for e in eps_in]
+        case = "elastic"
+    l = [math.log(max(f, 0.01)) for f in F]
+    ls = sum(l)
+    tau = [2 * mu * li + lam * ls for li in l]
+    return F, tau, case
+
+
+def jelly(eps, mu, lam):
+    F = [math.exp(e) for e in eps]
+    J = F[0] * F[1] * F[2]
+    tau = [2 * mu * (F[i] - 1.0) * F[i] + lam * J * (J - 1.0) for i in range(3)]
+    return F, tau, "elastic"
+
+
+def diag9(d):
+    return [d[0], 0.0, 0.0, 0.0, d[1], 0.0, 0.0, 0.0, d[2]]
+
+
+def make_return_map():
+    cases = []
+    strains = [
+        [0.0, 0.0, 0.0], [0.01, -0.02, 0.005], [-0.01, -0.01, -0.01], [0.02, 0.02, 0.02],
+        [-0.05, 0.01, 0.0], [-0.2, -0.05, 0.03], [0.1, -0.3, -0.1], [-0.001, 0.0005, 0.0002],
+        [0.05, -0.02, -0.04], [-0.15, -0.15, 0.1],
+    ]
+    for E, nu, phi in [(2e5, 0.3, 30.0), (3e5, 0.3, 35.0)]:
+        mu, lam = lame(E, nu)
+        al = alpha(phi)
+        for eps in strains:
+            F, tau, case = sand(eps, mu, lam, al)
+            cases.append(dict(material="sand", E=E, nu=nu, friction_angle=phi, yield_stress=0.0,
+                              F_trial=diag9([math.exp(e) for e in eps]), F=diag9(F),
+                              stress=diag9(tau), case=case))
+    mu, lam = lame(1e7, 0.3)
+    for eps in strains:
+        F, tau, case = metal(eps, mu, lam, 1e5)
+        cases.append(dict(material="metal", E=1e7, nu=0.3, friction_angle=30.0, yield_stress=1e5,
+                          F_trial=diag9([math.exp(e) for e in eps]), F=diag9(F),
+                          stress=diag9(tau), case=case))
+    mu, lam = lame(2e5, 0.3)
+    for eps in strains:
+        F, tau, case = jelly(eps, mu, lam)
+        cases.append(dict(material="jelly", E=2e5, nu=0.3, friction_angle=30.0, yield_stress=0.0,
+                          F_trial=diag9([math.exp(e) for e in eps]), F=diag9(F),
+                          stress=diag9(tau), case=case))
+    return cases
+
+
+def make_p2g():
+    """One particle, n_grid 16, dx 1/16: per-node (mass, momentum) contributions."""
+    n, lim = 16, 1.0
+    dx = lim / n
+    inv_dx = n / lim
+    x = [0.4137, 0.5261, 0.3319]
+    v = [0.3, -0.2, 0.1]
+    Cm = [0.5, -0.1, 0.2, 0.05, -0.3, 0.1, 0.0, 0.2, -0.4]
+    tau = [1200.0, 300.0, -150.0, 300.0, -800.0, 50.0, -150.0, 50.0, 400.0]
+    m, vol, dt = 2.0e-4, 1.0e-7, 1e-4
+    base, fx = [], []
+    for d in range(3):
+        gp = x[d] * inv_dx
+        b = int(gp - 0.5)
+        base.append(b)
+        fx.append(gp - b)
+    w = [[0.5 * (1.5 - f) ** 2, 0.75 - (f - 1.0) ** 2, 0.5 * (f - 0.5) ** 2] for f in fx]
+    dw = [[f - 1.5, -2.0 * (f - 1.0), f - 0.5] for f in fx]
+    nodes = []
+    for i in range(3):
+        for j in range(3):
+            for k in range(3):
+                wt = w[0][i] * w[1][j] * w[2][k]
+                gw = [dw[0][i] * w[1][j] * w[2][k] * inv_dx, w[0][i] * dw[1][j] * w[2][k] * inv_dx,
+                      w[0][i] * w[1][j] * dw[2][k] * inv_dx]
+                dpos = [(i - fx[0]) * dx, (j - fx[1]) * dx, (k - fx[2]) * dx]
+                mom = []
+                for r in range(3):
+                    cd = sum(Cm[3 * r + c] * dpos[c] for c in range(3))
+                    f = sum(-vol * tau[3 * r + c] * gw[c] for c in range(3))
+                    mom.append(wt * m * (v[r] + cd) + dt * f)
+                nodes.append(dict(index=[base[0] + i, base[1] + j, base[2] + k], mass=wt * m,
+                                  momentum=mom))
+    return dict(n_grid=n, grid_lim=lim, x=x, v=v, C=Cm, stress=tau, mass=m, vol=vol, dt=dt,
+                nodes=nodes)
+
+
+if __name__ == "__main__":
+    with open(os.path.join(HERE, "kat_return_map.json"), "w") as f:
+        json.dump(make_return_map(), f, indent=1)
+    with open(os.path.join(HERE, "kat_p2g.json"), "w") as f:
+        json.dump(make_p2g(), f, indent=1)
+    print("wrote kat_return_map.json, kat_p2g.json")

@@ -1,0 +1,78 @@
+"""Shared builders for the parity tests: a GPU simulator and its oracle twin
+started from the same seeded scene."""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from oracle import oracle as O
+from reduced_mpm_stress_training_gb300 import MPM_Simulator_WARP
+from reduced_mpm_stress_training_gb300 import scenarios as S
+
+
+def rel(a, b) -> float:
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def gpu_sim(sc: S.Scene, device="cuda:0", chunk_size=128, resort_interval=16, x0=None, v0=None,
+            vol=None, mass=None, colliders=True):
+    if x0 is None:
+        x0, v0, vol, mass = sc.particles()
+    sim = MPM_Simulator_WARP(sc.n_particles, n_grid=sc.n_grid, grid_lim=sc.grid_lim,
+                             device=device, chunk_size=chunk_size,
+                             resort_interval=resort_interval)
+    sim.set_parameters(material=sc.material, E=sc.E, nu=sc.nu,
+                       friction_angle=sc.friction_angle, gravity=sc.gravity,
+                       hardening=sc.hardening, xi=sc.xi)
+    if sc.material == "metal":
+        sim.set_parameters(yield_stress=sc.yield_stress)
+    sim.load_x_initial_from_tensor(torch.from_numpy(x0))
+    sim.load_vol_from_tensor(torch.from_numpy(vol))
+    sim.load_mass_from_tensor(torch.from_numpy(mass))
+    sim.load_v_from_tensor(torch.from_numpy(v0))
+    if colliders:
+        for kind, kw in sc.colliders():
+            if kind == "surface":
+                sim.add_surface_collider(**kw)
+            else:
+                sim.add_bounding_box(**kw)
+    return sim
+
+
+def oracle_sim(sc: S.Scene, bits=32, x0=None, v0=None, vol=None, mass=None, colliders=True):
+    if x0 is None:
+        x0, v0, vol, mass = sc.particles()
+    m = O.make_model(sc.n_grid, sc.grid_lim, material=sc.material, E=sc.E, nu=sc.nu,
+                     friction_angle=sc.friction_angle, gravity=sc.gravity,
+                     hardening=sc.hardening, xi=sc.xi)
+    cols = []
+    if colliders:
+        for kind, kw in sc.colliders():
+            cols.append(O.surface_collider(**kw) if kind == "surface" else O.bounding_box(**kw))
+    return O.OracleSim(m, x0, mass, vol, v0, bits=bits, colliders=cols,
+                       yield_stress=sc.yield_stress if sc.material == "metal" else None)
+
+
+def gpu_state(sim) -> dict:
+    n = sim.n_particles
+    e = sim._engine
+    from reduced_mpm_stress_training_gb300 import _capi as A
+
+    out = {}
+    for name, f in (("u", A.FIELD_U), ("v", A.FIELD_V), ("C", A.FIELD_C), ("F", A.FIELD_F),
+                    ("stress", A.FIELD_STRESS), ("x", A.FIELD_X), ("yield_", A.FIELD_YIELD)):
+        out[name] = e.export(f).cpu().numpy().reshape(n, -1)
+    return out
+
+
+def compare(sim, ref, fields=("x", "v", "C", "F", "stress")) -> dict:
+    """Relative L2 errors GPU vs oracle; "x" is x0 + u on both sides (u alone is
+    small early on, so its relative error is dominated by float32 rounding of x)."""
+    g = gpu_state(sim)
+    out = {}
+    for f in fields:
+        r = (ref.x0 + ref.u) if f == "x" else getattr(ref, f)
+        out[f] = rel(g[f], r.reshape(sim.n_particles, -1))
+    return out

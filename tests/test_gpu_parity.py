@@ -1,0 +1,243 @@
+"""GPU-vs-oracle parity of every stage of the substep, called through the
+C ABI (libmpm_gb300.so) on seeded inputs.
+
+Tolerances (relative L2 over all particles / nodes):
+  per substep: 1e-5 on grid mass/momentum/velocity and particle u, v, F, C, stress
+  200-substep sand rollout: 1e-4 on u and F (x = x0 + u)
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from reduced_mpm_stress_training_gb300 import _capi as A
+from reduced_mpm_stress_training_gb300 import scenarios as S
+from reduced_mpm_stress_training_gb300.engine import MPMStatusError, SceneParams
+
+from helpers import compare, gpu_sim, oracle_sim, rel
+
+pytestmark = pytest.mark.gpu
+
+TOL_STEP = 1e-5
+TOL_ROLLOUT = 1e-4
+
+
+def _rand_F(n, rng, kind):
+    if kind == "near_identity":
+        return (np.eye(3)[None] + 0.02 * rng.normal(size=(n, 3, 3))).astype(np.float32)
+    if kind == "compressed":
+        # rotations times diag(exp(s)), s in [-0.3, 0.05]: exercises all DP branches
+        q = rng.normal(size=(n, 4))
+        q /= np.linalg.norm(q, axis=1, keepdims=True)
+        w, x, y, z = q.T
+        R = np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                      2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                      2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], 1).reshape(n, 3, 3)
+        s = rng.uniform(-0.3, 0.05, size=(n, 3))
+        q2 = rng.normal(size=(n, 4))
+        q2 /= np.linalg.norm(q2, axis=1, keepdims=True)
+        w, x, y, z = q2.T
+        R2 = np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                       2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                       2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], 1).reshape(n, 3, 3)
+        return np.einsum("nij,nj,nkj->nik", R, np.exp(s), R2).astype(np.float32)
+    return rng.normal(size=(n, 3, 3)).astype(np.float32)
+
+
+@pytest.mark.parametrize("kind", ["random", "near_identity", "compressed"])
+def test_svd3_matches_oracle(cuda, kind):
+    rng = np.random.default_rng(1)
+    n = 20000
+    Fh = _rand_F(n, rng, kind).reshape(n, 9)
+    lib = A.load()
+    F = torch.from_numpy(Fh).to(cuda)
+    U = torch.empty_like(F)
+    V = torch.empty_like(F)
+    s = torch.empty((n, 3), device=cuda)
+    A.check(lib.mpm_svd3(F.data_ptr(), U.data_ptr(), s.data_ptr(), V.data_ptr(), n, 0), "svd")
+    torch.cuda.synchronize()
+    Ug, sg, Vg = (t.cpu().numpy().astype(np.float64) for t in (U, s, V))
+    Ug, Vg = Ug.reshape(n, 3, 3), Vg.reshape(n, 3, 3)
+    Uo, so, Vo = O.svd3(Fh, 32)
+    # reconstruction, orthogonality, convention
+    R = np.einsum("nij,nj,nkj->nik", Ug, sg, Vg)
+    scale = np.linalg.norm(Fh.reshape(n, 3, 3), axis=(1, 2))
+    assert np.max(np.linalg.norm(R - Fh.reshape(n, 3, 3), axis=(1, 2)) / scale) < 2e-5
+    assert np.abs(np.einsum("nji,njk->nik", Ug, Ug) - np.eye(3)).max() < 2e-6
+    assert np.abs(np.linalg.det(Ug) - 1).max() < 2e-6 and np.abs(np.linalg.det(Vg) - 1).max() < 2e-6
+    assert np.all(np.sign(sg[:, 2]) == np.sign(np.linalg.det(Fh.reshape(n, 3, 3))))
+    # singular values agree with the oracle's float32 SVD
+    assert np.max(np.abs(sg - so) / np.abs(so[:, :1])) < 1e-5
+
+
+def _scene_struct(material, mu, lam, friction=30.0, hardening=0, xi=0.0):
+    sp = SceneParams(n_particles=0, n_grid=8, material=material, mu=mu, lam=lam,
+                     friction_angle=friction, hardening=hardening, xi=xi)
+    return sp.to_struct(0)
+
+
+@pytest.mark.parametrize("material,kind", [(A.SAND, "near_identity"), (A.SAND, "compressed"),
+                                           (A.METAL, "near_identity"), (A.METAL, "compressed"),
+                                           (A.JELLY, "near_identity")])
+def test_return_map_matches_oracle(cuda, material, kind):
+    rng = np.random.default_rng(2)
+    n = 20000
+    Ft = _rand_F(n, rng, kind).reshape(n, 9)
+    E, nu = (2e5, 0.3) if material != A.METAL else (1e7, 0.3)
+    mu, lam = E / 2 / (1 + nu), E * nu / (1 + nu) / (1 - 2 * nu)
+    ys = 1e5
+    sc = _scene_struct(material, mu, lam, hardening=1 if material == A.METAL else 0, xi=0.5)
+    lib = A.load()
+    Fd = torch.from_numpy(Ft).to(cuda)
+    Fo = torch.empty_like(Fd)
+    tau = torch.empty_like(Fd)
+    y = torch.full((n,), ys, device=cuda)
+    A.check(lib.mpm_return_map(C.byref(sc), Fd.data_ptr(), y.data_ptr(), Fo.data_ptr(),
+                               tau.data_ptr(), n, 0), "return_map")
+    torch.cuda.synchronize()
+    mat = {A.SAND: "sand", A.METAL: "metal", A.JELLY: "jelly"}[material]
+    m = O.make_model(8, material=mat, mu=mu, lam=lam, friction_angle=30.0,
+                     hardening=1 if material == A.METAL else 0, xi=0.5)
+    Fr, tr, yr = O.return_map(m, Ft, yield_stress=ys, bits=32)
+    assert rel(Fo.cpu().numpy(), Fr) < TOL_STEP
+    assert rel(tau.cpu().numpy(), tr) < TOL_STEP
+    if material == A.METAL:
+        assert rel(y.cpu().numpy(), yr) < TOL_STEP
+
+
+def _perturbed_pair(sc, seed=3):
+    """GPU sim + oracle with non-trivial v, C and stress so every P2G term is exercised."""
+    rng = np.random.default_rng(seed)
+    x0, v0, vol, mass = sc.particles()
+    n = sc.n_particles
+    v0 = (0.1 * rng.normal(size=(n, 3))).astype(np.float32)
+    Cm = (0.5 * rng.normal(size=(n, 9))).astype(np.float32)
+    tau = (1e3 * rng.normal(size=(n, 9))).astype(np.float32)
+    sim = gpu_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass)
+    sim.load_C_from_tensor(torch.from_numpy(Cm))
+    sim.load_uvstress_from_tensor(torch.zeros(n, 3), torch.from_numpy(v0), torch.from_numpy(tau))
+    ref = oracle_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass)
+    ref.C[:] = Cm
+    ref.stress[:] = tau
+    return sim, ref
+
+
+def test_p2g_grid_matches_oracle(cuda):
+    sc = S.small_column(8192, 32)
+    sim, ref = _perturbed_pair(sc)
+    e = sim._engine
+    e.stage("sort")
+    e.stage("p2g", dt=sc.dt)
+    gm, gvin, _ = e.export_grid(0)
+    torch.cuda.synchronize()
+    ref.stage_p2g(sc.dt)
+    assert rel(gm.cpu().numpy(), ref.grid_m) < TOL_STEP
+    assert rel(gvin.cpu().numpy(), ref.grid_v_in) < TOL_STEP
+    # mass conservation (partition of unity)
+    assert abs(float(gm.double().sum()) / float(ref.mass.astype(np.float64).sum()) - 1) < 1e-5
+    e.stage("grid", time=0.0, dt=sc.dt)
+    _, _, gvout = e.export_grid(0)
+    torch.cuda.synchronize()
+    ref.stage_grid(sc.dt)
+    assert rel(gvout.cpu().numpy(), ref.grid_v_out) < TOL_STEP
+    e.stage("g2p", dt=sc.dt)
+    torch.cuda.synchronize()
+    ref.stage_g2p(sc.dt)
+    errs = compare(sim, ref)
+    assert all(v < TOL_STEP for v in errs.values()), errs
+
+
+@pytest.mark.parametrize("material", ["sand", "metal", "jelly"])
+def test_substeps_match_oracle(cuda, material):
+    sc = S.small_column(8192, 32, material=material)
+    sim = gpu_sim(sc)
+    ref = oracle_sim(sc)
+    for k in range(10):
+        sim.p2g2p(k, sc.dt)
+        ref.p2g2p(sc.dt)
+        errs = compare(sim, ref, fields=("x", "v", "F"))
+        assert all(v < TOL_STEP for v in errs.values()), (k, errs)
+    assert sim.check_status() == 0
+    if material == "metal":
+        assert rel(sim._engine.export(A.FIELD_YIELD).cpu().numpy(), ref.yield_) < TOL_STEP
+
+
+def test_sand_column_32k_rollout(cuda):
+    """The 32,768-particle 64^3 sand column, 200 substeps at dt 1e-4."""
+    sc = S.sand_column_32k()
+    sim = gpu_sim(sc)
+    ref = oracle_sim(sc)
+    ref64 = oracle_sim(sc, bits=64)
+    for k in range(sc.substeps):
+        sim.p2g2p(k, sc.dt)
+        ref.p2g2p(sc.dt)
+        ref64.p2g2p(sc.dt)
+    assert sim.check_status() == 0
+    errs = compare(sim, ref)
+    errs64 = compare(sim, ref64)
+    spread = {f: rel(getattr(ref, f), getattr(ref64, f)) for f in ("v", "F", "stress")}
+    print("gpu vs oracle32", errs, "gpu vs oracle64", errs64, "oracle32 vs oracle64", spread)
+    assert errs["x"] < TOL_ROLLOUT and errs["F"] < TOL_ROLLOUT
+    g = sim.mpm_state.particle_x.cpu().numpy()
+    assert rel(g, ref.x0 + ref.u) < TOL_ROLLOUT
+
+
+def test_out_of_domain_particle_is_flagged_not_fatal(cuda):
+    sc = S.small_column(1024, 32)
+    x0, v0, vol, mass = sc.particles()
+    x0[5] = (0.99, 0.5, 0.5)  # base index 31 > n-3: stencil leaves the 32^3 grid
+    sim = gpu_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass)
+    sim.p2g2p(0, sc.dt)
+    with pytest.raises(MPMStatusError) as ei:
+        sim.check_status()
+    assert ei.value.bits & A.ST_OUT_OF_DOMAIN
+    # the particle is frozen, the rest advanced normally
+    sim.on_error = "ignore"
+    ref = oracle_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass)
+    ref.p2g2p(sc.dt)
+    errs = compare(sim, ref, fields=("x", "v", "F"))
+    assert all(v < TOL_STEP for v in errs.values()), errs
+
+
+def test_cfl_violation_flagged(cuda):
+    sc = S.small_column(1024, 32)
+    x0, v0, vol, mass = sc.particles()
+    v0[:] = (0.0, 0.0, -400.0)  # dx/dt = (1/32)/1e-4 = 312.5
+    sim = gpu_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass, colliders=False)
+    sim.p2g2p(0, sc.dt)
+    with pytest.raises(MPMStatusError) as ei:
+        sim.check_status()
+    assert ei.value.bits & A.ST_CFL
+
+
+@pytest.mark.parametrize("n", [0, 1, 33])
+def test_tiny_particle_counts(cuda, n):
+    sc = S.small_column(max(n, 1), 16)
+    x0, v0, vol, mass = sc.particles()
+    x0, v0, vol, mass = x0[:n], v0[:n], vol[:n], mass[:n]
+    sc.n_particles = n
+    sim = gpu_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass)
+    for k in range(3):
+        sim.p2g2p(k, sc.dt)
+    assert sim.check_status() == 0
+    if n:
+        ref = oracle_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass)
+        for _ in range(3):
+            ref.p2g2p(sc.dt)
+        errs = compare(sim, ref, fields=("x", "v", "F"))
+        assert all(v < TOL_STEP for v in errs.values()), errs
+
+
+@pytest.mark.parametrize("chunk", [32, 64, 256])
+@pytest.mark.parametrize("resort", [0, 1, 7])
+def test_chunk_size_and_resort_do_not_change_results(cuda, chunk, resort):
+    sc = S.small_column(4096, 32)
+    sim = gpu_sim(sc, chunk_size=chunk, resort_interval=resort)
+    ref = oracle_sim(sc)
+    for k in range(6):
+        sim.p2g2p(k, sc.dt)
+        ref.p2g2p(sc.dt)
+    errs = compare(sim, ref, fields=("x", "v", "F", "stress"))
+    assert all(v < TOL_STEP for v in errs.values()), errs
