@@ -41,8 +41,8 @@ constexpr int kStateFloatArrays = 3 + 3 + 3 + 9 + 9 + 9 + 1 + 1 + 1;  // 39
 constexpr int kStateArrays = kStateFloatArrays + 2;
 
 struct WsLayout {
-    int64_t order, counts, offsets, cursor, tile_sums, ticket, chunks, n_chunks, grid_acc, grid_v,
-        block_flag, active_list, n_active, n_active_prev, staging, total;
+    int64_t order, counts, offsets, cursor, tile_sums, ticket, chunks, n_chunks, blocks, n_blocks,
+        grid_acc, grid_v, block_flag, active_list, n_active, n_active_prev, staging, total;
     int nbk, n_tiles;
 };
 
@@ -58,10 +58,12 @@ WsLayout ws_layout(const MpmPlan &p) {
     L.counts = take(nbk * 4);
     L.offsets = take(nbk * 4);
     L.cursor = take(nbk * 4);
-    L.tile_sums = take((int64_t)L.n_tiles * 8);
+    L.tile_sums = take((int64_t)L.n_tiles * 16);
     L.ticket = take(4);
     L.chunks = take(p.max_chunks * 16);
     L.n_chunks = take(4);
+    L.blocks = take((p.total_blocks + 1) * 16);
+    L.n_blocks = take(4);
     L.grid_acc = take(p.total_blocks * mpm::kBlockNodes * 16);
     L.grid_v = take(p.total_blocks * mpm::kBlockNodes * 16);
     L.block_flag = take(p.total_blocks * 4);
@@ -104,10 +106,12 @@ mpm::Ctx make_ctx(const MpmBuffers *b, void *stream, int which) {
     ws.counts = reinterpret_cast<int *>(w + L.counts);
     ws.offsets = reinterpret_cast<int *>(w + L.offsets);
     ws.cursor = reinterpret_cast<int *>(w + L.cursor);
-    ws.tile_sums = reinterpret_cast<int2 *>(w + L.tile_sums);
+    ws.tile_sums = reinterpret_cast<int4 *>(w + L.tile_sums);
     ws.ticket = reinterpret_cast<unsigned *>(w + L.ticket);
     ws.chunks = reinterpret_cast<int4 *>(w + L.chunks);
     ws.n_chunks = reinterpret_cast<int *>(w + L.n_chunks);
+    ws.blocks = reinterpret_cast<int4 *>(w + L.blocks);
+    ws.n_blocks = reinterpret_cast<int *>(w + L.n_blocks);
     ws.grid_acc = reinterpret_cast<float4 *>(w + L.grid_acc);
     ws.grid_v = reinterpret_cast<float4 *>(w + L.grid_v);
     ws.block_flag = reinterpret_cast<int *>(w + L.block_flag);
@@ -119,6 +123,7 @@ mpm::Ctx make_ctx(const MpmBuffers *b, void *stream, int which) {
     ws.n_tiles = L.n_tiles;
     ws.max_chunks = (int)p.max_chunks;
     ws.chunk_size = p.chunk_size;
+    ws.n = (int)p.n_particles;
     cx.n = (int)p.n_particles;
     cx.status = b->status;
     cx.stream = static_cast<cudaStream_t>(stream);

@@ -28,10 +28,12 @@ struct PState {  // one particle-state buffer, SoA, component stride `stride`
 
 struct Ws {  // workspace
     int *order, *counts, *offsets, *cursor;
-    int2 *tile_sums;
+    int4 *tile_sums;  // per scan tile: (particles, chunks, non-empty blocks)
     unsigned *ticket;
-    int4 *chunks;     // (global block, start, count, scene)
+    int4 *chunks;     // G2P work: (global block, start, count <= chunk_size, scene)
     int *n_chunks;
+    int4 *blocks;     // P2G work: (global block, start, count, scene), one per non-empty block
+    int *n_blocks;
     float4 *grid_acc; // (momentum xyz, mass), block-major
     float4 *grid_v;   // (velocity xyz, mass) after the grid update
     int *block_flag;
@@ -43,6 +45,7 @@ struct Ws {  // workspace
     int n_tiles;
     int max_chunks;
     int chunk_size;
+    int n;            // particles (bounds every order[] index)
 };
 
 // ---------------------------------------------------------------------------

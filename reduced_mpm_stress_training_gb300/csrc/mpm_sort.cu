@@ -37,103 +37,108 @@ __global__ void key_kernel(const MpmScene *__restrict__ scenes, int n_scenes, PS
     warp_histogram(ws.counts, key);
 }
 
-// Phase 1: per-tile sums of (count, ceil(count/chunk)).  The last CTA
-// (atomic ticket; nobody waits) scans the tile sums into exclusive offsets
-// and publishes the chunk total.
+__device__ __forceinline__ int4 add4(int4 a, int4 b) {
+    return make_int4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+// inclusive scan of an int4 triple over the 256 threads of a CTA; returns the
+// thread's inclusive value and leaves the CTA total in *total (shared)
+__device__ __forceinline__ int4 cta_scan4(int4 v, int4 *wsum /* [8] shared */, int4 &total) {
+    int4 x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int4 y;
+        y.x = __shfl_up_sync(0xffffffffu, x.x, o);
+        y.y = __shfl_up_sync(0xffffffffu, x.y, o);
+        y.z = __shfl_up_sync(0xffffffffu, x.z, o);
+        y.w = 0;
+        if ((threadIdx.x & 31) >= o) x = add4(x, y);
+    }
+    if ((threadIdx.x & 31) == 31) wsum[threadIdx.x >> 5] = x;
+    __syncthreads();
+    int4 pre = make_int4(0, 0, 0, 0);
+    total = make_int4(0, 0, 0, 0);
+    for (int w = 0; w < 8; ++w) {
+        if (w < (int)(threadIdx.x >> 5)) pre = add4(pre, wsum[w]);
+        total = add4(total, wsum[w]);
+    }
+    __syncthreads();
+    return add4(pre, x);
+}
+
+// per-bucket triple: (particles, G2P chunks, non-empty) -- the sentinel
+// bucket (out-of-domain particles) contributes particles only
+__device__ __forceinline__ int4 bucket_triple(const Ws &ws, int b, int cnt) {
+    if (b >= ws.nbk - 1) return make_int4(cnt, 0, 0, 0);
+    return make_int4(cnt, (cnt + ws.chunk_size - 1) / ws.chunk_size, cnt > 0 ? 1 : 0, 0);
+}
+
+// Phase 1: per-tile sums.  The last CTA to finish (atomic ticket; nobody
+// waits) scans the tile sums into exclusive tile offsets and publishes the
+// work-list lengths.
 __global__ void __launch_bounds__(256) scan_tiles_kernel(Ws ws) {
-    __shared__ int2 red[8];
+    __shared__ int4 wsum[8];
     __shared__ bool last;
     const int tile = blockIdx.x;
     const int b0 = tile * kScanTile + threadIdx.x * 8;
-    const int cs = ws.chunk_size;
-    int c = 0, k = 0;
+    int4 acc = make_int4(0, 0, 0, 0);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         int b = b0 + j;
-        if (b < ws.nbk - 1) {  // the sentinel bucket gets no chunks
-            int v = ws.counts[b];
-            c += v;
-            k += (v + cs - 1) / cs;
-        } else if (b == ws.nbk - 1) {
-            c += ws.counts[b];
-        }
+        if (b < ws.nbk) acc = add4(acc, bucket_triple(ws, b, ws.counts[b]));
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        c += __shfl_down_sync(0xffffffffu, c, o);
-        k += __shfl_down_sync(0xffffffffu, k, o);
-    }
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_int2(c, k);
-    __syncthreads();
+    int4 total;
+    cta_scan4(acc, wsum, total);
     if (threadIdx.x == 0) {
-        int2 s = make_int2(0, 0);
-        for (int w = 0; w < 8; ++w) { s.x += red[w].x; s.y += red[w].y; }
-        ws.tile_sums[tile] = s;
+        ws.tile_sums[tile] = total;
         __threadfence();
         unsigned t = atomicAdd(ws.ticket, 1u);
         last = (t == (unsigned)gridDim.x - 1);
     }
     __syncthreads();
     if (!last) return;
-    // last CTA: exclusive scan of the tile sums (n_tiles <= a few thousand)
     __threadfence();
-    __shared__ int2 carry;
-    if (threadIdx.x == 0) carry = make_int2(0, 0);
-    __syncthreads();
+    int4 carry = make_int4(0, 0, 0, 0);
     for (int base = 0; base < ws.n_tiles; base += 256) {
-        int t = base + threadIdx.x;
-        int2 v = t < ws.n_tiles ? __ldcg(ws.tile_sums + t) : make_int2(0, 0);
-        int x = v.x, y = v.y;
-        // inclusive warp scan
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int xs = __shfl_up_sync(0xffffffffu, x, o), ys = __shfl_up_sync(0xffffffffu, y, o);
-            if ((threadIdx.x & 31) >= o) { x += xs; y += ys; }
+        const int t = base + threadIdx.x;
+        int4 v = t < ws.n_tiles ? __ldcg(ws.tile_sums + t) : make_int4(0, 0, 0, 0);
+        int4 tot;
+        int4 inc = cta_scan4(v, wsum, tot);
+        if (t < ws.n_tiles) {
+            int4 ex = add4(carry, make_int4(inc.x - v.x, inc.y - v.y, inc.z - v.z, 0));
+            ws.tile_sums[t] = ex;
         }
-        __shared__ int2 wsum[8];
-        if ((threadIdx.x & 31) == 31) wsum[threadIdx.x >> 5] = make_int2(x, y);
-        __syncthreads();
-        int2 pre = carry;
-        for (int w = 0; w < (threadIdx.x >> 5); ++w) { pre.x += wsum[w].x; pre.y += wsum[w].y; }
-        if (t < ws.n_tiles) ws.tile_sums[t] = make_int2(pre.x + x - v.x, pre.y + y - v.y);
-        __syncthreads();
-        if (threadIdx.x == 255) carry = make_int2(pre.x + x, pre.y + y);
-        __syncthreads();
+        carry = add4(carry, tot);
     }
     if (threadIdx.x == 0) {
-        *ws.n_chunks = carry.y;
+        // counts always sum to n when the stages run in order; the clamps keep
+        // a mis-sequenced call from walking past the work lists
+        *ws.n_chunks = min(carry.y, ws.max_chunks);
+        *ws.n_blocks = min(carry.z, ws.nbk - 1);
         *ws.ticket = 0u;  // re-arm for the next substep
     }
 }
 
-// Phase 2: bucket offsets / cursors, chunk list, zero the histogram.
+// Phase 2: bucket offsets / cursors, the G2P chunk list and the P2G block
+// list; zeroes the histogram for the next substep.
 __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__restrict__ scenes,
                                                           int n_scenes, Ws ws) {
+    __shared__ int4 wsum[8];
     const int tile = blockIdx.x;
     const int b0 = tile * kScanTile + threadIdx.x * 8;
     const int cs = ws.chunk_size;
     int cnt[8];
-    int c = 0, k = 0;
+    int4 acc = make_int4(0, 0, 0, 0);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         int b = b0 + j;
         cnt[j] = b < ws.nbk ? ws.counts[b] : 0;
-        c += cnt[j];
-        if (b < ws.nbk - 1) k += (cnt[j] + cs - 1) / cs;
+        if (b < ws.nbk) acc = add4(acc, bucket_triple(ws, b, cnt[j]));
     }
-    // block-wide exclusive scan of (c, k)
-    int x = c, y = k;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int xs = __shfl_up_sync(0xffffffffu, x, o), ys = __shfl_up_sync(0xffffffffu, y, o);
-        if ((threadIdx.x & 31) >= o) { x += xs; y += ys; }
-    }
-    __shared__ int2 wsum[8];
-    if ((threadIdx.x & 31) == 31) wsum[threadIdx.x >> 5] = make_int2(x, y);
-    __syncthreads();
-    int2 pre = ws.tile_sums[tile];
-    for (int w = 0; w < (threadIdx.x >> 5); ++w) { pre.x += wsum[w].x; pre.y += wsum[w].y; }
-    int off = pre.x + x - c, coff = pre.y + y - k;
+    int4 total;
+    int4 inc = cta_scan4(acc, wsum, total);
+    const int4 pre = ws.tile_sums[tile];
+    int off = pre.x + inc.x - acc.x, coff = pre.y + inc.y - acc.y, boff = pre.z + inc.z - acc.z;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         int b = b0 + j;
@@ -142,7 +147,9 @@ __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__rest
         ws.cursor[b] = off;
         ws.counts[b] = 0;
         if (b < ws.nbk - 1 && cnt[j] > 0) {
-            int sc = scene_of_block(scenes, n_scenes, b);
+            const int sc = scene_of_block(scenes, n_scenes, b);
+            if (boff < ws.nbk - 1) ws.blocks[boff] = make_int4(b, off, cnt[j], sc);
+            ++boff;
             for (int s = 0; s < cnt[j]; s += cs) {
                 if (coff < ws.max_chunks)
                     ws.chunks[coff] = make_int4(b, off + s, min(cs, cnt[j] - s), sc);
@@ -172,7 +179,8 @@ __global__ void scatter_kernel(PState st, Ws ws, int n) {
     int base = 0;
     if (key >= 0 && lane == leader) base = atomicAdd(ws.cursor + key, __popc(peers));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (key >= 0) ws.order[base + __popc(peers & ((1u << lane) - 1u))] = i;
+    const int pos = base + __popc(peers & ((1u << lane) - 1u));
+    if (key >= 0 && pos < n) ws.order[pos] = i;
 }
 
 // physical re-sort: dst[i] = src[order[i]] for every field; order := identity

@@ -36,87 +36,209 @@ __device__ __forceinline__ void chunk_block(const MpmScene &S, int gblock, int &
 // ---------------------------------------------------------------------------
 // P2G: p2g_apic_stress_given, engine_stress/mpm_utils.py:190-227
 //   grid_v_in += (w m)(v + C dpos) + dt (-vol tau) grad w,  grid_m += w m
+//
+// One warp per non-empty grid block, with a warp-private 6x6x6 node tile in
+// shared memory and no floating-point atomics in the particle loop:
+//   (a) classify the block's particles by cell (64 cells), int shared atomics
+//       give each particle its rank within its cell;
+//   (b,c) counting sort by cell;
+//   (d) order "layer-major": layer r holds the r-th particle of every cell,
+//       so a window of 32 consecutive particles has (almost always) 32
+//       distinct cells, and their stencils hit distinct nodes for every node
+//       offset -- plain read-modify-writes of the tile are race-free;
+//   (e) per window, the rare lanes that share a cell (windows spanning two
+//       short layers) are serialised by __match_any_sync rank;
+//   flush: one float4 atomicAdd per non-zero tile node into the global grid.
+// Blocks with more than kPassCap particles are processed in passes.
 // ---------------------------------------------------------------------------
-template <int CH>
-__global__ void __launch_bounds__(CH) p2g_kernel(const MpmScene *__restrict__ scenes, PState st,
-                                                 Ws ws, float dt, int *status) {
-    __shared__ float tile[kTileNodes * 4];
-    const int n_chunks = *ws.n_chunks;
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        const int4 ch = ws.chunks[c];
-        for (int i = threadIdx.x; i < kTileNodes * 4; i += CH) tile[i] = 0.0f;
-        __syncthreads();
-        const MpmScene &S = scenes[ch.w];
-        int bx, by, bz;
-        chunk_block(S, ch.x, bx, by, bz);
-        if (threadIdx.x < ch.z) {
-            const int slot = ws.order[ch.y + threadIdx.x];
-            const int64_t sd = st.stride;
-            float gp[3];
-            int base[3];
-            bool ok = true;
+constexpr int kP2GWarps = 4;
+constexpr int kPassCap = 256;
+
+struct P2GWarpSmem {
+    float4 tile[kTileNodes];
+    int cnt[64];
+    int cstart[64];
+    int sorted[kPassCap];
+    unsigned short perm[kPassCap];
+    unsigned short tmpr[kPassCap];
+    unsigned char tmpc[kPassCap];
+};
+
+struct P2GParticle {
+    Weights W;
+    int lx, ly, lz;
+    float m;
+    float a0[3];  // v - C fx dx
+    float Cd[9];  // C dx
+    float T[9];   // -dt vol inv_dx tau
+};
+
+__device__ __forceinline__ bool p2g_load(const MpmScene &S, const PState &st, int slot, int bx,
+                                         int by, int bz, float dt, P2GParticle &P) {
+    const int64_t sd = st.stride;
+    float gp[3];
+    int base[3];
+    bool ok = true;
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                gp[d] = grid_coord(st.x0[slot + d * sd], st.u[slot + d * sd], S.inv_dx);
-                ok &= stencil_base(gp[d], S.n_grid, base[d]);
-            }
-            const int lx = base[0] - 4 * bx, ly = base[1] - 4 * by, lz = base[2] - 4 * bz;
-            ok &= (unsigned)lx < 4u && (unsigned)ly < 4u && (unsigned)lz < 4u;
-            if (!ok) {
-                atomicOr(status, MPM_ST_INTERNAL);
-            } else {
-                Weights W;
-                make_weights(gp, base, W);
-                const float m = st.mass[slot], vol = st.vol[slot];
-                const float dx = S.dx;
-                float Cm[9], T[9], a0[3];
+    for (int d = 0; d < 3; ++d) {
+        gp[d] = grid_coord(st.x0[slot + d * sd], st.u[slot + d * sd], S.inv_dx);
+        ok &= stencil_base(gp[d], S.n_grid, base[d]);
+    }
+    P.lx = base[0] - 4 * bx;
+    P.ly = base[1] - 4 * by;
+    P.lz = base[2] - 4 * bz;
+    ok &= (unsigned)P.lx < 4u && (unsigned)P.ly < 4u && (unsigned)P.lz < 4u;
+    if (!ok) return false;
+    make_weights(gp, base, P.W);
+    P.m = st.mass[slot];
+    const float vol = st.vol[slot];
+    const float dx = S.dx;
+    float Cm[9];
 #pragma unroll
-                for (int k = 0; k < 9; ++k) Cm[k] = st.C[slot + k * sd];
-                // force term: dt * (-vol tau) * grad w, grad w = inv_dx * (...)
-                const float tscale = -vol * dt * S.inv_dx;
+    for (int k = 0; k < 9; ++k) Cm[k] = st.C[slot + k * sd];
+    const float tscale = -vol * dt * S.inv_dx;
 #pragma unroll
-                for (int k = 0; k < 9; ++k) T[k] = st.tau[slot + k * sd] * tscale;
-                // momentum term: (w m)(v + C (ijk - fx) dx) = (w m)(a0 + C ijk dx)
+    for (int k = 0; k < 9; ++k) P.T[k] = st.tau[slot + k * sd] * tscale;
 #pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    float cf = Cm[r * 3 + 0] * W.fx[0] + Cm[r * 3 + 1] * W.fx[1] + Cm[r * 3 + 2] * W.fx[2];
-                    a0[r] = st.v[slot + r * sd] - cf * dx;
-                }
+    for (int r = 0; r < 3; ++r) {
+        const float cf = Cm[r * 3 + 0] * P.W.fx[0] + Cm[r * 3 + 1] * P.W.fx[1] + Cm[r * 3 + 2] * P.W.fx[2];
+        P.a0[r] = st.v[slot + r * sd] - cf * dx;
+    }
 #pragma unroll
-                for (int k = 0; k < 9; ++k) Cm[k] *= dx;
+    for (int k = 0; k < 9; ++k) P.Cd[k] = Cm[k] * dx;
+    return true;
+}
+
+// add one particle's 27 node contributions into the tile (read-modify-write)
+__device__ __forceinline__ void p2g_scatter(const P2GParticle &P, float4 *tile, unsigned mask) {
 #pragma unroll
-                for (int i = 0; i < 3; ++i) {
+    for (int i = 0; i < 3; ++i) {
 #pragma unroll
-                    for (int j = 0; j < 3; ++j) {
-                        const float p1 = W.dw[0][i] * W.w[1][j];
-                        const float p2 = W.w[0][i] * W.dw[1][j];
-                        const float p3 = W.w[0][i] * W.w[1][j];
-                        float aij[3];
+        for (int j = 0; j < 3; ++j) {
+            const float p1 = P.W.dw[0][i] * P.W.w[1][j];
+            const float p2 = P.W.w[0][i] * P.W.dw[1][j];
+            const float p3 = P.W.w[0][i] * P.W.w[1][j];
+            float aij[3];
 #pragma unroll
-                        for (int r = 0; r < 3; ++r)
-                            aij[r] = a0[r] + (float)i * Cm[r * 3 + 0] + (float)j * Cm[r * 3 + 1];
+            for (int r = 0; r < 3; ++r)
+                aij[r] = P.a0[r] + (float)i * P.Cd[r * 3 + 0] + (float)j * P.Cd[r * 3 + 1];
 #pragma unroll
-                        for (int k = 0; k < 3; ++k) {
-                            const float w = p3 * W.w[2][k];
-                            const float wm = w * m;
-                            const float g0 = p1 * W.w[2][k], g1 = p2 * W.w[2][k], g2 = p3 * W.dw[2][k];
-                            float* t = tile + 4 * (((lx + i) * kTile + (ly + j)) * kTile + (lz + k));
+            for (int k = 0; k < 3; ++k) {
+                const float w = p3 * P.W.w[2][k];
+                const float wm = w * P.m;
+                const float g0 = p1 * P.W.w[2][k], g1 = p2 * P.W.w[2][k], g2 = p3 * P.W.dw[2][k];
+                float add[3];
 #pragma unroll
-                            for (int r = 0; r < 3; ++r) {
-                                float mom = wm * (aij[r] + (float)k * Cm[r * 3 + 2]);
-                                float f = T[r * 3 + 0] * g0 + T[r * 3 + 1] * g1 + T[r * 3 + 2] * g2;
-                                atomicAdd(t + r, mom + f);
-                            }
-                            atomicAdd(t + 3, wm);
-                        }
-                    }
-                }
+                for (int r = 0; r < 3; ++r)
+                    add[r] = wm * (aij[r] + (float)k * P.Cd[r * 3 + 2]) +
+                             (P.T[r * 3 + 0] * g0 + P.T[r * 3 + 1] * g1 + P.T[r * 3 + 2] * g2);
+                float4 *t = tile + ((P.lx + i) * kTile + (P.ly + j)) * kTile + (P.lz + k);
+                float4 o = *t;
+                o.x += add[0];
+                o.y += add[1];
+                o.z += add[2];
+                o.w += wm;
+                *t = o;
+                __syncwarp(mask);
             }
         }
-        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kP2GWarps * 32) p2g_kernel(const MpmScene *__restrict__ scenes,
+                                                             PState st, Ws ws, float dt,
+                                                             int *status) {
+    __shared__ P2GWarpSmem smem[kP2GWarps];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    P2GWarpSmem &sm = smem[threadIdx.x >> 5];
+    const int nblk = *ws.n_blocks;
+    for (int bi = blockIdx.x * kP2GWarps + (int)(threadIdx.x >> 5); bi < nblk;
+         bi += gridDim.x * kP2GWarps) {
+        const int4 be = ws.blocks[bi];
+        const MpmScene &S = scenes[be.w];
+        int bx, by, bz;
+        chunk_block(S, be.x, bx, by, bz);
+        for (int i = lane; i < kTileNodes; i += 32) sm.tile[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int p0 = 0; p0 < be.z; p0 += kPassCap) {
+            const int np = min(kPassCap, be.z - p0);
+            sm.cnt[lane] = 0;
+            sm.cnt[lane + 32] = 0;
+            __syncwarp();
+            // (a) classify by cell
+            for (int i = lane; i < np; i += 32) {
+                const int idx = be.y + p0 + i;
+                int c = 255;
+                if (idx < ws.n) {
+                    const int slot = ws.order[idx];
+                    const int64_t sd = st.stride;
+                    int base[3];
+                    bool ok = true;
+#pragma unroll
+                    for (int d = 0; d < 3; ++d)
+                        ok &= stencil_base(grid_coord(st.x0[slot + d * sd], st.u[slot + d * sd], S.inv_dx),
+                                           S.n_grid, base[d]);
+                    const int lx = base[0] - 4 * bx, ly = base[1] - 4 * by, lz = base[2] - 4 * bz;
+                    ok &= (unsigned)lx < 4u && (unsigned)ly < 4u && (unsigned)lz < 4u;
+                    if (ok) c = (lx * 4 + ly) * 4 + lz;
+                    else atomicOr(status, MPM_ST_INTERNAL);
+                }
+                sm.tmpc[i] = (unsigned char)c;
+                if (c != 255) sm.tmpr[i] = (unsigned short)atomicAdd(&sm.cnt[c], 1);
+            }
+            __syncwarp();
+            // (b) cell offsets (exclusive scan over 64 cells, two per lane)
+            const int c0 = sm.cnt[lane], c1 = sm.cnt[lane + 32];
+            int s0 = c0, s1 = c1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y0 = __shfl_up_sync(full, s0, o), y1 = __shfl_up_sync(full, s1, o);
+                if (lane >= o) { s0 += y0; s1 += y1; }
+            }
+            const int tot0 = __shfl_sync(full, s0, 31);
+            sm.cstart[lane] = s0 - c0;
+            sm.cstart[lane + 32] = tot0 + s1 - c1;
+            const int maxcnt = __reduce_max_sync(full, max(c0, c1));
+            __syncwarp();
+            // (c) cell-sorted slots
+            for (int i = lane; i < np; i += 32) {
+                const int c = sm.tmpc[i];
+                if (c != 255) sm.sorted[sm.cstart[c] + sm.tmpr[i]] = ws.order[be.y + p0 + i];
+            }
+            // (d) layer-major permutation
+            int nv = 0;
+            for (int r = 0; r < maxcnt; ++r) {
+                const bool a = c0 > r, b = c1 > r;
+                const unsigned ma = __ballot_sync(full, a), mb = __ballot_sync(full, b);
+                if (a) sm.perm[nv + __popc(ma & lt)] = (unsigned short)(sm.cstart[lane] + r);
+                if (b) sm.perm[nv + __popc(ma) + __popc(mb & lt)] = (unsigned short)(sm.cstart[lane + 32] + r);
+                nv += __popc(ma) + __popc(mb);
+            }
+            __syncwarp();
+            // (e) windows of 32 particles
+            for (int w0 = 0; w0 < nv; w0 += 32) {
+                const int k = w0 + lane;
+                bool act = k < nv;
+                P2GParticle P;
+                if (act) act = p2g_load(S, st, sm.sorted[sm.perm[k]], bx, by, bz, dt, P);
+                const int cell = act ? (P.lx * 4 + P.ly) * 4 + P.lz : -1 - lane;
+                const unsigned peers = __match_any_sync(full, cell);
+                const int rank = act ? __popc(peers & lt) : 0;
+                const int npass = __reduce_max_sync(full, rank) + 1;
+                for (int q = 0; q < npass; ++q) {
+                    const bool go = act && rank == q;
+                    const unsigned gm = __ballot_sync(full, go);
+                    if (go) p2g_scatter(P, sm.tile, gm);
+                    __syncwarp();
+                }
+            }
+            __syncwarp();
+        }
+        // flush the tile: one float4 atomic per non-zero node
         const int nb = S.n_blocks_axis;
-        for (int i = threadIdx.x; i < kTileNodes; i += CH) {
-            float4 a = reinterpret_cast<float4 *>(tile)[i];
+        for (int i = lane; i < kTileNodes; i += 32) {
+            const float4 a = sm.tile[i];
             if (a.x != 0.0f || a.y != 0.0f || a.z != 0.0f || a.w != 0.0f) {
                 const int tx = i / 36, ty = (i / 6) % 6, tz = i % 6;
                 const int ix = 4 * bx + tx, iy = 4 * by + ty, iz = 4 * bz + tz;
@@ -124,16 +246,15 @@ __global__ void __launch_bounds__(CH) p2g_kernel(const MpmScene *__restrict__ sc
                     atomicAdd(ws.grid_acc + node_addr(S.block_begin, nb, ix, iy, iz), a);
             }
         }
-        if (threadIdx.x < 8) {
-            const int gx = bx + (threadIdx.x >> 2), gy = by + ((threadIdx.x >> 1) & 1),
-                      gz = bz + (threadIdx.x & 1);
+        if (lane < 8) {
+            const int gx = bx + (lane >> 2), gy = by + ((lane >> 1) & 1), gz = bz + (lane & 1);
             if (gx < nb && gy < nb && gz < nb) {
                 const int gb = (int)(S.block_begin + ((int64_t)(gx * nb + gy) * nb + gz));
                 if (atomicExch(ws.block_flag + gb, 1) == 0)
                     ws.active_list[atomicAdd(ws.n_active, 1)] = gb;
             }
         }
-        __syncthreads();
+        __syncwarp();
     }
 }
 
@@ -213,7 +334,7 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
         }
         __syncthreads();
         int key = -1;
-        if (threadIdx.x < ch.z) {
+        if (threadIdx.x < ch.z && ch.y + (int)threadIdx.x < ws.n) {
             const int slot = ws.order[ch.y + threadIdx.x];
             const int64_t sd = st.stride;
             float x0[3], gp[3], xo[3];
@@ -320,11 +441,6 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
 }
 
 template <int CH>
-static cudaError_t p2g_t(const Ctx &cx, float dt, int grid) {
-    p2g_kernel<CH><<<grid, CH, 0, cx.stream>>>(cx.scenes, cx.st, cx.ws, dt, cx.status);
-    return cudaGetLastError();
-}
-template <int CH>
 static cudaError_t g2p_t(const Ctx &cx, float dt, int grid) {
     g2p_kernel<CH><<<grid, CH, 0, cx.stream>>>(cx.scenes, cx.st, cx.ws, dt, cx.status);
     return cudaGetLastError();
@@ -336,14 +452,12 @@ static int persistent_grid(const Ctx &cx, int per_sm) {
 }
 
 cudaError_t launch_p2g(const Ctx &cx, float dt) {
-    const int grid = persistent_grid(cx, 2048 / cx.ws.chunk_size);
-    switch (cx.ws.chunk_size) {
-        case 32: return p2g_t<32>(cx, dt, grid);
-        case 64: return p2g_t<64>(cx, dt, grid);
-        case 128: return p2g_t<128>(cx, dt, grid);
-        case 256: return p2g_t<256>(cx, dt, grid);
-        default: return cudaErrorInvalidValue;
-    }
+    // persistent: enough warps to fill every SM, never more than the blocks
+    int64_t want = (cx.total_blocks + kP2GWarps - 1) / kP2GWarps;
+    int grid = (int)(want < (int64_t)cx.num_sms * 6 ? want : (int64_t)cx.num_sms * 6);
+    if (grid < 1) grid = 1;
+    p2g_kernel<<<grid, kP2GWarps * 32, 0, cx.stream>>>(cx.scenes, cx.st, cx.ws, dt, cx.status);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_grid(const Ctx &cx, float time, float dt) {
