@@ -1,0 +1,398 @@
+"""Throughput benchmark of the GB300 MPM substep (MPM_Simulator_WARP.p2g2p).
+
+Workload (default): the large sand column -- 1,048,576 sand particles,
+128^3 grid (dx = 1/128), column [0.35,0.65]^2 x [0.05,0.85], Drucker-Prager
+E = 2e5, nu = 0.3, friction 30 deg, density 2200, gravity (0,0,-9.8),
+sticky floor + slip walls, dt = 5e-5.  Seeded synthetic particles (the
+reference's sampling data is not available).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One JSON line on rank 0.  A "step" is one substep of every particle.
+  value  -- particle-substeps/s with the state resident in HBM, substeps
+            replayed from a CUDA graph, timed with CUDA events (max over ranks)
+  e2e    -- the same metric through the C ABI with host buffers: each step
+            loads u, v, stress from pinned host memory (load_uvstress_from_tensor),
+            runs the substep and reads u, v, F_disp, stress back to pinned host
+            memory (export_uvFstress_from_warp)
+  --impl reference -- the CPU restatement of the reference's algorithm (the
+            reference is Python + Warp and cannot be installed here) on all
+            host cores, on a bounded particle sample per step.
+Multi-GPU: independent replicas, one per rank (the substep has no
+cross-GPU exchange); value sums all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALG_BYTES = {"sand": 284, "jelly": 284, "metal": 288}  # per particle-substep
+METRIC = "particle-substeps/s (1M sand, fp32)"
+
+
+def workload_config(sc, world: int) -> dict:
+    return {"workload": f"{sc.name}: {sc.n_particles} particles, {sc.n_grid}^3 grid, dt {sc.dt}, "
+                        f"{sc.material}, sticky floor + slip walls",
+            "particles": sc.n_particles, "grid": sc.n_grid, "parallelism": f"replicas x{world}"}
+
+
+KERNEL_BYTES = {"p2g": 116, "g2p": 192}  # algorithmic particle bytes per launch unit
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="sand_column_1m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(value: float, world: int, device) -> float:
+    """Max of a host float over all ranks (identity for one rank)."""
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int, device=None):
+    if world > 1:
+        import torch.distributed as dist
+
+        if device is not None and device.type == "cuda":
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "100"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, copy)"
+    except Exception:
+        return 6800.0, "fallback (6.8 TB/s)"
+
+
+def profiled_traffic(workload: str):
+    """Per-substep DRAM bytes from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"dram_traffic_{workload}.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+def cpu_port_rate(sc, n_sample: int, min_seconds: float, max_steps: int, steps: int | None = None):
+    """Particle-substeps/s of the CPU restatement (all host threads) on the
+    first n_sample particles of the scene's seeded set."""
+    from oracle import oracle as O
+
+    x0, v0, vol, mass = sc.particles()
+    x0, v0, vol, mass = (a[:n_sample].copy() for a in (x0, v0, vol, mass))
+    m = O.make_model(sc.n_grid, sc.grid_lim, material=sc.material, E=sc.E, nu=sc.nu,
+                     friction_angle=sc.friction_angle, gravity=sc.gravity)
+    cols = [O.surface_collider(**kw) if k == "surface" else O.bounding_box(**kw)
+            for k, kw in sc.colliders()]
+    sim = O.OracleSim(m, x0, mass, vol, v0, bits=32, colliders=cols,
+                      yield_stress=sc.yield_stress if sc.material == "metal" else None)
+    nt = O.max_threads()
+    sim.p2g2p(sc.dt, nthreads_p2g=nt)  # warm
+    done, t0 = 0, time.perf_counter()
+    while True:
+        sim.p2g2p(sc.dt, nthreads_p2g=nt)
+        done += 1
+        el = time.perf_counter() - t0
+        if steps is not None:
+            if done >= steps:
+                break
+        elif (el >= min_seconds and done >= 2) or done >= max_steps:
+            break
+    return n_sample * done / el, nt, done, el
+
+
+def reference_arm(args, sc, world, rank):
+    if rank != 0:
+        return
+    # bound the per-step sample so K steps end within about two minutes
+    from oracle import oracle as O  # noqa: F401
+
+    probe = 65536
+    rate, nt, _, _ = cpu_port_rate(sc, probe, 0.0, 2, steps=2)
+    per_step_budget = 120.0 / max(1, args.steps + args.warmup)
+    n_sample = int(max(4096, min(sc.n_particles, rate * per_step_budget)))
+    n_sample = 1 << int(math.log2(n_sample))
+    rate, nt, done, el = cpu_port_rate(sc, n_sample, 0.0, 0, steps=args.steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate,
+        "unit": "particle-substeps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(sc, args.gpus),
+        "cpu_baseline": {"value": rate, "unit": "particle-substeps/s", "cores": nt, "kind": "port",
+                         "sample": f"first {n_sample} particles of the seeded {sc.n_particles}-particle "
+                                   f"column on the {sc.n_grid}^3 grid, one substep per step "
+                                   "(C restatement of the reference's Warp kernels, float32, OpenMP)"},
+        "e2e": {"value": rate, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "reference is Python + NVIDIA Warp; warp-lang is not installable offline, "
+                "so the reference arm times the project's C restatement of its algorithm",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def gb300_arm(args, sc, world, rank, local):
+    import torch
+
+    from reduced_mpm_stress_training_gb300 import _capi as A
+    from reduced_mpm_stress_training_gb300.scenarios import build_simulator
+
+    device = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(device)
+    resort = 16
+    sim = build_simulator(sc, device=device, resort_interval=resort)
+    eng = sim._engine
+    n = sc.n_particles
+    dt = sc.dt
+    W = max(3, args.warmup)
+    for k in range(W):
+        sim.p2g2p(k, dt)
+    torch.cuda.synchronize()
+    sim.check_status()
+
+    gsize = 2 * resort
+    graph = eng.graph(gsize, float(sim.time), dt)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    K = args.steps
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(device.index if world == 1 else local)
+    barrier(world, device)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(st)
+    for _ in range(K // gsize):
+        graph.replay()
+    for _ in range(K % gsize):
+        eng.substep_raw(float(sim.time), dt)
+    ev1.record(st)
+    torch.cuda.synchronize()
+    barrier(world, device)
+    clk = clocks.stop()
+    t = ev0.elapsed_time(ev1) / 1e3
+    t_max = max_over_ranks(t, world, device)
+    status = eng.status()
+    launches_per_substep = 6 + 1.0 / resort  # 3 sort + p2g + grid + g2p (+ periodic re-sort)
+    value = world * n * K / t_max
+    ms_per_step = 1e3 * t_max / K
+
+    # per-stage times, eager, CUDA events on the launching stream
+    stage_ms = {"sort": 0.0, "p2g": 0.0, "grid": 0.0, "g2p": 0.0}
+    reps = 32
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    for k in range(reps):
+        evs[0].record(st)
+        eng.stage("sort")
+        evs[1].record(st)
+        eng.stage("p2g", dt=dt)
+        evs[2].record(st)
+        eng.stage("grid", time=float(sim.time), dt=dt)
+        evs[3].record(st)
+        eng.stage("g2p", dt=dt)
+        evs[4].record(st)
+        torch.cuda.synchronize()
+        for i, kname in enumerate(stage_ms):
+            stage_ms[kname] += evs[i].elapsed_time(evs[i + 1]) / reps
+
+    # end to end through the C ABI with pinned host buffers
+    hu = torch.empty(n * 3, dtype=torch.float32).pin_memory()
+    hv = torch.empty(n * 3, dtype=torch.float32).pin_memory()
+    hs = torch.empty(n * 9, dtype=torch.float32).pin_memory()
+    eng.export(A.FIELD_U, hu)
+    eng.export(A.FIELD_V, hv)
+    eng.export(A.FIELD_STRESS, hs)
+    ou = torch.empty(n * 3, dtype=torch.float32).pin_memory()
+    ov = torch.empty(n * 3, dtype=torch.float32).pin_memory()
+    of = torch.empty(n * 9, dtype=torch.float32).pin_memory()
+    os_ = torch.empty(n * 9, dtype=torch.float32).pin_memory()
+    k_e2e = max(3, min(K, 100))
+
+    def e2e_step():
+        eng.load_host(A.FIELD_U, hu)
+        eng.load_host(A.FIELD_V, hv)
+        eng.load_host(A.FIELD_STRESS, hs)
+        eng.substep_raw(float(sim.time), dt)
+        eng.export(A.FIELD_U, ou)
+        eng.export(A.FIELD_V, ov)
+        eng.export(A.FIELD_F_DISP, of)
+        eng.export(A.FIELD_STRESS, os_)
+
+    for _ in range(3):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world, device)
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        e2e_step()
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world, device)
+    e2e_value = world * n * k_e2e / t_e2e
+    status |= eng.status()
+
+    if rank != 0:
+        return
+    peak, peak_src = measured_peak_hbm()
+    alg = ALG_BYTES[sc.material]
+    achieved = alg * n / (t_max / K) / 1e9
+    traffic = profiled_traffic(sc.name)
+    kern = {}
+    for kname, b in KERNEL_BYTES.items():
+        ms = stage_ms[kname]
+        gbs = b * n / (ms * 1e-3) / 1e9
+        kern[kname] = {"ms": round(ms, 4), "algorithmic_bytes": b * n, "achieved_gbs": round(gbs, 1),
+                       "frac": round(gbs / peak, 4)}
+    for kname in ("sort", "grid"):
+        kern[kname] = {"ms": round(stage_ms[kname], 4)}
+    line = {
+        "metric": METRIC, "value": value,
+        "unit": "particle-substeps/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded uniform particles in the column; reference sampling data absent)",
+        "config": dict(workload_config(sc, world),
+                       l2="state larger than L2 (2 x %.0f MB particle buffers + grid); no flush"
+                          % (eng.plan.state_bytes / 1e6),
+                       timing=f"CUDA graph of {gsize} substeps replayed, CUDA events"),
+        "roofline": {"bound": "hbm", "kernel": "substep (sort + p2g + grid + g2p)",
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4),
+                     "traffic": None if traffic is None else traffic.get("bytes_per_substep"),
+                     "algorithmic_bytes_per_unit": alg, "unit_count": n, "peak_source": peak_src},
+        "roofline_kernels": kern,
+        "e2e": {"value": e2e_value, "unit": "particle-substeps/s", "h2d_bytes_per_step": 60 * n,
+                "d2h_bytes_per_step": 96 * n, "steps": k_e2e},
+        "gpu_launches": int(round(K * launches_per_substep)),
+        "clocks": clk,
+        "status": status,
+    }
+    if not args.no_cpu_baseline:
+        rate, nt, done, el = cpu_port_rate(sc, sc.n_particles, 10.0, 30)
+        line["cpu_baseline"] = {"value": rate, "unit": "particle-substeps/s", "cores": nt,
+                                "kind": "port",
+                                "sample": f"{done} substeps of the full {sc.n_particles}-particle "
+                                          f"column ({el:.1f} s), C restatement (float32, OpenMP)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    from reduced_mpm_stress_training_gb300 import scenarios as S
+
+    sc = S.SCENES[args.workload]()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        if args.impl == "reference":
+            if rank != 0:
+                return
+        else:
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    if args.impl == "reference":
+        reference_arm(args, sc, world, rank)
+        return
+    if world == 1:
+        import __graft_entry__ as g
+
+        g.build()
+    gb300_arm(args, sc, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -13,7 +13,8 @@ namespace mpm {
 constexpr int kTile = 6;                // padded node tile per 4^3-cell block
 constexpr int kTileNodes = kTile * kTile * kTile;  // 216
 constexpr int kBlockNodes = 64;         // nodes of one 4x4x4 grid block
-constexpr int kScanTile = 2048;         // buckets per scan CTA (256 threads x 8)
+constexpr int kScanPerThread = 2;      // buckets per scan thread
+constexpr int kScanTile = 256 * kScanPerThread;  // buckets per scan CTA
 constexpr int kSvdSweeps = 5;           // Jacobi sweeps (converged in float32)
 
 // ---------------------------------------------------------------------------

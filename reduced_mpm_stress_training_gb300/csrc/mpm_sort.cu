@@ -80,10 +80,10 @@ __global__ void __launch_bounds__(256) scan_tiles_kernel(Ws ws) {
     __shared__ int4 wsum[8];
     __shared__ bool last;
     const int tile = blockIdx.x;
-    const int b0 = tile * kScanTile + threadIdx.x * 8;
+    const int b0 = tile * kScanTile + threadIdx.x * kScanPerThread;
     int4 acc = make_int4(0, 0, 0, 0);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < kScanPerThread; ++j) {
         int b = b0 + j;
         if (b < ws.nbk) acc = add4(acc, bucket_triple(ws, b, ws.counts[b]));
     }
@@ -125,12 +125,12 @@ __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__rest
                                                           int n_scenes, Ws ws) {
     __shared__ int4 wsum[8];
     const int tile = blockIdx.x;
-    const int b0 = tile * kScanTile + threadIdx.x * 8;
+    const int b0 = tile * kScanTile + threadIdx.x * kScanPerThread;
     const int cs = ws.chunk_size;
-    int cnt[8];
+    int cnt[kScanPerThread];
     int4 acc = make_int4(0, 0, 0, 0);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < kScanPerThread; ++j) {
         int b = b0 + j;
         cnt[j] = b < ws.nbk ? ws.counts[b] : 0;
         if (b < ws.nbk) acc = add4(acc, bucket_triple(ws, b, cnt[j]));
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__rest
     const int4 pre = ws.tile_sums[tile];
     int off = pre.x + inc.x - acc.x, coff = pre.y + inc.y - acc.y, boff = pre.z + inc.z - acc.z;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < kScanPerThread; ++j) {
         int b = b0 + j;
         if (b >= ws.nbk) break;
         ws.offsets[b] = off;

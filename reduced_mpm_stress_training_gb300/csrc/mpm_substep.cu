@@ -52,7 +52,7 @@ __device__ __forceinline__ void chunk_block(const MpmScene &S, int gblock, int &
 // Blocks with more than kPassCap particles are processed in passes.
 // ---------------------------------------------------------------------------
 constexpr int kP2GWarps = 4;
-constexpr int kPassCap = 256;
+constexpr int kPassCap = 512;
 
 struct P2GWarpSmem {
     float4 tile[kTileNodes];
@@ -109,7 +109,11 @@ __device__ __forceinline__ bool p2g_load(const MpmScene &S, const PState &st, in
     return true;
 }
 
-// add one particle's 27 node contributions into the tile (read-modify-write)
+// add one particle's 27 node contributions into the tile (read-modify-write).
+// Per (i,j) the node value factors over k:
+//   add_r = wz_k A_r + k wz_k B_r + dwz_k D_r,  mass = pm wz_k
+// with pm = wx_i wy_j m, A_r = pm (a0_r + i Cdx_r + j Cdy_r) + T_r0 dwx_i wy_j
+// + T_r1 wx_i dwy_j, B_r = pm Cdz_r, D_r = T_r2 wx_i wy_j.
 __device__ __forceinline__ void p2g_scatter(const P2GParticle &P, float4 *tile, unsigned mask) {
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -118,34 +122,32 @@ __device__ __forceinline__ void p2g_scatter(const P2GParticle &P, float4 *tile, 
             const float p1 = P.W.dw[0][i] * P.W.w[1][j];
             const float p2 = P.W.w[0][i] * P.W.dw[1][j];
             const float p3 = P.W.w[0][i] * P.W.w[1][j];
-            float aij[3];
+            const float pm = p3 * P.m;
+            float A[3], B[3], D[3];
 #pragma unroll
-            for (int r = 0; r < 3; ++r)
-                aij[r] = P.a0[r] + (float)i * P.Cd[r * 3 + 0] + (float)j * P.Cd[r * 3 + 1];
+            for (int r = 0; r < 3; ++r) {
+                const float aij = P.a0[r] + (float)i * P.Cd[r * 3 + 0] + (float)j * P.Cd[r * 3 + 1];
+                A[r] = pm * aij + P.T[r * 3 + 0] * p1 + P.T[r * 3 + 1] * p2;
+                B[r] = pm * P.Cd[r * 3 + 2];
+                D[r] = P.T[r * 3 + 2] * p3;
+            }
+            float4 *t = tile + ((P.lx + i) * kTile + (P.ly + j)) * kTile + P.lz;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const float w = p3 * P.W.w[2][k];
-                const float wm = w * P.m;
-                const float g0 = p1 * P.W.w[2][k], g1 = p2 * P.W.w[2][k], g2 = p3 * P.W.dw[2][k];
-                float add[3];
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    add[r] = wm * (aij[r] + (float)k * P.Cd[r * 3 + 2]) +
-                             (P.T[r * 3 + 0] * g0 + P.T[r * 3 + 1] * g1 + P.T[r * 3 + 2] * g2);
-                float4 *t = tile + ((P.lx + i) * kTile + (P.ly + j)) * kTile + (P.lz + k);
-                float4 o = *t;
-                o.x += add[0];
-                o.y += add[1];
-                o.z += add[2];
-                o.w += wm;
-                *t = o;
+                const float wz = P.W.w[2][k], dwz = P.W.dw[2][k], kwz = (float)k * wz;
+                float4 o = t[k];
+                o.x += wz * A[0] + kwz * B[0] + dwz * D[0];
+                o.y += wz * A[1] + kwz * B[1] + dwz * D[1];
+                o.z += wz * A[2] + kwz * B[2] + dwz * D[2];
+                o.w += pm * wz;
+                t[k] = o;
                 __syncwarp(mask);
             }
         }
     }
 }
 
-__global__ void __launch_bounds__(kP2GWarps * 32) p2g_kernel(const MpmScene *__restrict__ scenes,
+__global__ void __launch_bounds__(kP2GWarps * 32, 4) p2g_kernel(const MpmScene *__restrict__ scenes,
                                                              PState st, Ws ws, float dt,
                                                              int *status) {
     __shared__ P2GWarpSmem smem[kP2GWarps];
@@ -357,36 +359,60 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
                 Weights W;
                 make_weights(gp, base, W);
                 const float inv_dx = S.inv_dx;
-                float nv[3] = {0.f, 0.f, 0.f}, nC[9], nF[9];
+                // Separable gather (same sums as :261-273, regrouped by axis):
+                //   nv  = sum_ijk wx_i wy_j wz_k g
+                //   nF  = sum g (x) (dwx wy wz, wx dwy wz, wx wy dwz)   (times inv_dx)
+                //   M_c = sum (w g) * (ijk)_c,  C = 4 inv_dx (M - nv (x) fx)
+                // z first (S, D, K per (i,j)), then y, then x.
+                float nv[3] = {0.f, 0.f, 0.f}, nF[9], M[9];
 #pragma unroll
-                for (int k = 0; k < 9; ++k) { nC[k] = 0.f; nF[k] = 0.f; }
+                for (int k = 0; k < 9; ++k) { nF[k] = 0.f; M[k] = 0.f; }
 #pragma unroll
-                for (int i = 0; i < 3; ++i)
+                for (int i = 0; i < 3; ++i) {
+                    float Ti[3] = {0.f, 0.f, 0.f}, Ui[3] = {0.f, 0.f, 0.f}, Ri[3] = {0.f, 0.f, 0.f};
+                    float Ji[3] = {0.f, 0.f, 0.f}, Ki[3] = {0.f, 0.f, 0.f};
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
-                        const float p1 = W.dw[0][i] * W.w[1][j];
-                        const float p2 = W.w[0][i] * W.dw[1][j];
-                        const float p3 = W.w[0][i] * W.w[1][j];
+                        const float4 *row = tile + ((lx + i) * kTile + (ly + j)) * kTile + lz;
+                        const float4 g0 = row[0], g1 = row[1], g2 = row[2];
+                        const float gz[3][3] = {{g0.x, g0.y, g0.z}, {g1.x, g1.y, g1.z}, {g2.x, g2.y, g2.z}};
+                        float Sz[3], Dz[3], Kz[3];
 #pragma unroll
-                        for (int k = 0; k < 3; ++k) {
-                            const float4 g = tile[((lx + i) * kTile + (ly + j)) * kTile + (lz + k)];
-                            const float gv[3] = {g.x, g.y, g.z};
-                            const float w = p3 * W.w[2][k];
-                            const float dpos[3] = {(float)i - W.fx[0], (float)j - W.fx[1], (float)k - W.fx[2]};
-                            const float sc = w * inv_dx * 4.0f;
-                            const float dwt[3] = {p1 * W.w[2][k] * inv_dx, p2 * W.w[2][k] * inv_dx,
-                                                  p3 * W.dw[2][k] * inv_dx};
+                        for (int r = 0; r < 3; ++r) {
+                            Sz[r] = W.w[2][0] * gz[0][r] + W.w[2][1] * gz[1][r] + W.w[2][2] * gz[2][r];
+                            Dz[r] = W.dw[2][0] * gz[0][r] + W.dw[2][1] * gz[1][r] + W.dw[2][2] * gz[2][r];
+                            Kz[r] = W.w[2][1] * gz[1][r] + 2.0f * (W.w[2][2] * gz[2][r]);
+                        }
+                        const float wy = W.w[1][j], dwy = W.dw[1][j];
 #pragma unroll
-                            for (int r = 0; r < 3; ++r) {
-                                nv[r] += gv[r] * w;
-#pragma unroll
-                                for (int q = 0; q < 3; ++q) {
-                                    nC[r * 3 + q] += gv[r] * dpos[q] * sc;
-                                    nF[r * 3 + q] += gv[r] * dwt[q];
-                                }
-                            }
+                        for (int r = 0; r < 3; ++r) {
+                            Ti[r] += wy * Sz[r];
+                            Ui[r] += dwy * Sz[r];
+                            Ri[r] += wy * Dz[r];
+                            Ki[r] += wy * Kz[r];
+                            if (j > 0) Ji[r] += (float)j * (wy * Sz[r]);
                         }
                     }
+                    const float wx = W.w[0][i], dwx = W.dw[0][i];
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        nv[r] += wx * Ti[r];
+                        nF[r * 3 + 0] += dwx * Ti[r];
+                        nF[r * 3 + 1] += wx * Ui[r];
+                        nF[r * 3 + 2] += wx * Ri[r];
+                        if (i > 0) M[r * 3 + 0] += (float)i * (wx * Ti[r]);
+                        M[r * 3 + 1] += wx * Ji[r];
+                        M[r * 3 + 2] += wx * Ki[r];
+                    }
+                }
+                float nC[9];
+                const float c4 = 4.0f * inv_dx;
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) nC[r * 3 + q] = c4 * (M[r * 3 + q] - nv[r] * W.fx[q]);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) nF[k] *= inv_dx;
                 // x += dt v (:277), u = x - x0 (:12-15)
                 float un[3];
 #pragma unroll

@@ -271,6 +271,15 @@ class MPMEngine:
         A.check(self.lib.mpm_p2g2p(C.byref(self.buf), time, dt, self.stream), "mpm_p2g2p")
         self._queue_status()
 
+    def substep_raw(self, time: float, dt: float) -> None:
+        """One substep without the lazy status bookkeeping (safe inside a
+        CUDA-graph capture)."""
+        A.check(self.lib.mpm_p2g2p(C.byref(self.buf), time, dt, self.stream), "mpm_p2g2p")
+
+    def graph(self, n_substeps: int, time: float, dt: float) -> "SubstepGraph":
+        """Capture n_substeps substeps in one CUDA graph (see SubstepGraph)."""
+        return SubstepGraph(self, n_substeps, time, dt)
+
     def stage(self, name: str, time: float = 0.0, dt: float = 0.0) -> None:
         b = C.byref(self.buf)
         s = self.stream
@@ -316,3 +325,41 @@ class MPMEngine:
     def clear_status(self) -> None:
         self._status.zero_()
         self._pending = False
+
+
+class SubstepGraph:
+    """n substeps captured once in a CUDA graph and replayed.
+
+    The library's host-side control (live state buffer, substep counter) moves
+    as the substeps are recorded; a replay runs the recorded launches with the
+    recorded buffer pointers.  So n must contain an even number of physical
+    re-sorts (n a multiple of 2 * resort_interval, or resort_interval 0) and
+    the block keys must be valid when capturing (take one eager substep
+    first).  ``time`` is frozen at capture: colliders with finite time windows
+    need eager stepping.  The status word is not read inside the graph; call
+    ``engine.status()`` after replays.
+    """
+
+    def __init__(self, engine: MPMEngine, n: int, time: float, dt: float):
+        b = engine.buf
+        if not b.keys_valid:
+            raise RuntimeError("take one eager substep before capturing (block keys invalid)")
+        self.engine = engine
+        self.n = n
+        cur0, step0 = b.cur, b.substep
+        self.graph = torch.cuda.CUDAGraph()
+        stream = torch.cuda.Stream(engine.device)
+        stream.wait_stream(torch.cuda.current_stream(engine.device))
+        with torch.cuda.graph(self.graph, stream=stream):
+            for _ in range(n):
+                engine.substep_raw(time, dt)
+        if b.cur != cur0:
+            b.cur = cur0
+            b.substep = step0
+            raise ValueError("a captured window must contain an even number of re-sorts: "
+                             "use n a multiple of 2 * resort_interval")
+        b.substep = step0  # nothing has run yet
+
+    def replay(self) -> None:
+        self.graph.replay()
+        self.engine.buf.substep += self.n

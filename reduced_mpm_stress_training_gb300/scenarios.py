@@ -146,3 +146,28 @@ SCENES = {
     "metal_block_1m": metal_block_1m,
     "sand_rollout_131k": sand_rollout_131k,
 }
+
+
+def build_simulator(sc: Scene, device="cuda:0", chunk_size: int = 128, resort_interval: int = 16):
+    """An MPM_Simulator_WARP loaded with the scene (particles, material, colliders)."""
+    import torch
+
+    from .solver import MPM_Simulator_WARP
+
+    x0, v0, vol, mass = sc.particles()
+    sim = MPM_Simulator_WARP(sc.n_particles, n_grid=sc.n_grid, grid_lim=sc.grid_lim, device=device,
+                             chunk_size=chunk_size, resort_interval=resort_interval)
+    sim.set_parameters(material=sc.material, E=sc.E, nu=sc.nu, friction_angle=sc.friction_angle,
+                       gravity=sc.gravity, hardening=sc.hardening, xi=sc.xi)
+    if sc.material == "metal":
+        sim.set_parameters(yield_stress=sc.yield_stress)
+    sim.load_x_initial_from_tensor(torch.from_numpy(x0))
+    sim.load_vol_from_tensor(torch.from_numpy(vol))
+    sim.load_mass_from_tensor(torch.from_numpy(mass))
+    sim.load_v_from_tensor(torch.from_numpy(v0))
+    for kind, kw in sc.colliders():
+        if kind == "surface":
+            sim.add_surface_collider(**kw)
+        else:
+            sim.add_bounding_box(**kw)
+    return sim
