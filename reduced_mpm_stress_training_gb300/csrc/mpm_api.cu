@@ -36,13 +36,13 @@ int num_sms() {
 constexpr int64_t kAlign = 256;
 inline int64_t align_up(int64_t x, int64_t a = kAlign) { return (x + a - 1) / a * a; }
 
-// particle-state buffer: 39 float arrays then uid and key, each `stride` long
-constexpr int kStateFloatArrays = 3 + 3 + 3 + 9 + 9 + 9 + 1 + 1 + 1;  // 39
-constexpr int kStateArrays = kStateFloatArrays + 2;
+// particle-state buffer: `stride` records of 160 B, then `stride` int keys
+constexpr int64_t kStateBytesPerParticle = mpm::kRecWords * 4 + 4;
 
 struct WsLayout {
-    int64_t order, counts, offsets, cursor, tile_sums, ticket, chunks, n_chunks, blocks, n_blocks,
-        grid_acc, grid_v, block_flag, active_list, n_active, n_active_prev, staging, total;
+    int64_t order, counts, cell_counts, cell_start, cell_cursor, tile_sums, ticket, chunks, n_chunks,
+        blocks, n_blocks, grid_acc, grid_v, block_flag, active_list, n_active, n_active_prev, staging,
+        total;
     int nbk, n_tiles;
 };
 
@@ -56,8 +56,9 @@ WsLayout ws_layout(const MpmPlan &p) {
     auto take = [&](int64_t bytes) { int64_t at = o; o = align_up(o + bytes); return at; };
     L.order = take(n * 4);
     L.counts = take(nbk * 4);
-    L.offsets = take(nbk * 4);
-    L.cursor = take(nbk * 4);
+    L.cell_counts = take(nbk * 64 * 4);
+    L.cell_start = take(nbk * 64 * 4);
+    L.cell_cursor = take(nbk * 64 * 4);
     L.tile_sums = take((int64_t)L.n_tiles * 16);
     L.ticket = take(4);
     L.chunks = take(p.max_chunks * 16);
@@ -76,20 +77,10 @@ WsLayout ws_layout(const MpmPlan &p) {
 }
 
 mpm::PState state_view(void *base, int64_t stride) {
-    float *f = static_cast<float *>(base);
     mpm::PState s;
     s.stride = stride;
-    s.x0 = f;
-    s.u = f + 3 * stride;
-    s.v = f + 6 * stride;
-    s.C = f + 9 * stride;
-    s.F = f + 18 * stride;
-    s.tau = f + 27 * stride;
-    s.mass = f + 36 * stride;
-    s.vol = f + 37 * stride;
-    s.yld = f + 38 * stride;
-    s.uid = reinterpret_cast<int *>(f + 39 * stride);
-    s.key = reinterpret_cast<int *>(f + 40 * stride);
+    s.rec = static_cast<float4 *>(base);
+    s.key = reinterpret_cast<int *>(static_cast<char *>(base) + stride * mpm::kRecWords * 4);
     return s;
 }
 
@@ -104,8 +95,9 @@ mpm::Ctx make_ctx(const MpmBuffers *b, void *stream, int which) {
     mpm::Ws &ws = cx.ws;
     ws.order = reinterpret_cast<int *>(w + L.order);
     ws.counts = reinterpret_cast<int *>(w + L.counts);
-    ws.offsets = reinterpret_cast<int *>(w + L.offsets);
-    ws.cursor = reinterpret_cast<int *>(w + L.cursor);
+    ws.cell_counts = reinterpret_cast<int *>(w + L.cell_counts);
+    ws.cell_start = reinterpret_cast<int *>(w + L.cell_start);
+    ws.cell_cursor = reinterpret_cast<int *>(w + L.cell_cursor);
     ws.tile_sums = reinterpret_cast<int4 *>(w + L.tile_sums);
     ws.ticket = reinterpret_cast<unsigned *>(w + L.ticket);
     ws.chunks = reinterpret_cast<int4 *>(w + L.chunks);
@@ -183,7 +175,7 @@ int mpm_plan(MpmScene *scenes, int32_t n_scenes, int64_t n_particles, int32_t ch
         blocks += (int64_t)S.n_blocks_axis * S.n_blocks_axis * S.n_blocks_axis;
     }
     if (next_particle != n_particles) return MPM_ERR_ARG;
-    if (blocks >= ((int64_t)1 << 31) / mpm::kBlockNodes) return MPM_ERR_SIZE;
+    if (blocks + 1 >= ((int64_t)1 << 31) / mpm::kBlockNodes) return MPM_ERR_SIZE;
     MpmPlan p;
     memset(&p, 0, sizeof(p));
     p.n_particles = n_particles;
@@ -193,7 +185,7 @@ int mpm_plan(MpmScene *scenes, int32_t n_scenes, int64_t n_particles, int32_t ch
     p.n_scenes = n_scenes;
     const int64_t nonempty = n_particles < blocks ? n_particles : blocks;
     p.max_chunks = n_particles / chunk_size + nonempty + 1;
-    p.state_bytes = (int64_t)kStateArrays * p.particle_stride * 4;
+    p.state_bytes = kStateBytesPerParticle * p.particle_stride;
     p.workspace_bytes = ws_layout(p).total;
     *plan = p;
     return MPM_OK;
@@ -259,6 +251,7 @@ int mpm_sort(MpmBuffers *b, void *stream) {
     bool resort = false;
     if (!b->keys_valid) {
         MPM_CHECK(cudaMemsetAsync(cx.ws.counts, 0, (size_t)cx.ws.nbk * sizeof(int), cx.stream));
+        MPM_CHECK(cudaMemsetAsync(cx.ws.cell_counts, 0, (size_t)cx.ws.nbk * 64 * sizeof(int), cx.stream));
         MPM_CHECK(mpm::launch_keys(cx));
         b->keys_valid = 1;
         resort = true;

@@ -20,15 +20,48 @@ constexpr int kSvdSweeps = 5;           // Jacobi sweeps (converged in float32)
 // ---------------------------------------------------------------------------
 // Views of the caller's buffers (layout fixed by mpm_plan).
 // ---------------------------------------------------------------------------
-struct PState {  // one particle-state buffer, SoA, component stride `stride`
-    float *x0, *u, *v, *C, *F, *tau, *mass, *vol, *yld;
-    int *uid;  // user index of each slot
-    int *key;  // grid-block key of each slot for the coming sort
+// One particle-state buffer: a 160-byte record per slot (10 float4) plus a
+// cell-key array.  Record words (float unless noted):
+//   q0:  0-2 x_initial, 3 mass
+//   q1:  4 vol, 5 uid (int bits, the user's particle index), 6 yield_stress, 7 F[8]
+//   q2:  8-10 u, 11 v.x
+//   q3:  12-13 v.y v.z, 14-15 C[0..1]
+//   q4:  16-19 C[2..5]
+//   q5:  20-22 C[6..8], 23 stress[0]
+//   q6:  24-27 stress[1..4]
+//   q7:  28-31 stress[5..8]
+//   q8:  32-35 F[0..3]
+//   q9:  36-39 F[4..7]
+// P2G reads q0-q7 (128 B, four 32-byte sectors); G2P reads q0, q1, q2, q8,
+// q9 and writes q1-q9.  Matrices are row-major as in the reference.
+constexpr int kRecWords = 40;
+constexpr int kRecQuads = 10;
+namespace rec {
+constexpr int X0 = 0, MASS = 3, VOL = 4, UID = 5, YLD = 6, F8 = 7, U = 8, V = 11, C = 14,
+              TAU = 23, F0 = 32;
+}
+struct PState {
+    float4 *rec;  // n records (padded stride)
+    int *key;     // cell key (block * 64 + cell in block) of each slot for the coming sort
     int64_t stride;
 };
 
+__device__ __forceinline__ float4 ldrec(const PState &st, int slot, int q) {
+    return st.rec[(int64_t)slot * kRecQuads + q];
+}
+__device__ __forceinline__ void strec(const PState &st, int slot, int q, float4 v) {
+    st.rec[(int64_t)slot * kRecQuads + q] = v;
+}
+__device__ __forceinline__ float *recw(const PState &st, int slot) {
+    return reinterpret_cast<float *>(st.rec + (int64_t)slot * kRecQuads);
+}
+
 struct Ws {  // workspace
-    int *order, *counts, *offsets, *cursor;
+    int *order;        // sorted position -> slot
+    int *counts;       // particles per grid block (bucket), last = out of domain
+    int *cell_counts;  // particles per cell (64 per block)
+    int *cell_start;   // first sorted position of each cell
+    int *cell_cursor;  // scatter cursor of each cell; equals the cell end afterwards
     int4 *tile_sums;  // per scan tile: (particles, chunks, non-empty blocks)
     unsigned *ticket;
     int4 *chunks;     // G2P work: (global block, start, count <= chunk_size, scene)
@@ -113,24 +146,30 @@ __device__ __forceinline__ int scene_of_particle(const MpmScene *sc, int n_scene
     return lo;
 }
 
-// block key of a particle position: global block id or the sentinel (nbk-1)
+// cell key of a particle position: global block id * 64 + cell within the
+// block (base cell of the stencil), or sentinel_block * 64 when out of domain
 __device__ __forceinline__ int particle_key(const MpmScene &S, float x0x, float x0y, float x0z,
-                                            float ux, float uy, float uz, int sentinel, bool &ok) {
+                                            float ux, float uy, float uz, int sentinel_block,
+                                            bool &ok) {
     int bx, by, bz;
     bool a = stencil_base(grid_coord(x0x, ux, S.inv_dx), S.n_grid, bx);
     bool b = stencil_base(grid_coord(x0y, uy, S.inv_dx), S.n_grid, by);
     bool c = stencil_base(grid_coord(x0z, uz, S.inv_dx), S.n_grid, bz);
     ok = a && b && c;
     const int nb = S.n_blocks_axis;
-    return ok ? (int)(S.block_begin + ((int64_t)((bx >> 2) * nb + (by >> 2)) * nb + (bz >> 2)))
-              : sentinel;
+    const int blk = (int)(S.block_begin + ((int64_t)((bx >> 2) * nb + (by >> 2)) * nb + (bz >> 2)));
+    const int cell = ((bx & 3) << 4) | ((by & 3) << 2) | (bz & 3);
+    return ok ? blk * 64 + cell : sentinel_block * 64;
 }
 
-// warp-aggregated atomicAdd of 1 per lane into counts[key] (key < 0: skip)
-__device__ __forceinline__ void warp_histogram(int *counts, int key) {
+// warp-aggregated histogram of cell keys at block and cell level (key < 0: skip)
+__device__ __forceinline__ void warp_histogram(int *counts, int *cell_counts, int key) {
+    const int lane = threadIdx.x & 31;
     unsigned peers = __match_any_sync(0xffffffffu, key);
-    int leader = __ffs(peers) - 1;
-    if (key >= 0 && (threadIdx.x & 31) == leader) atomicAdd(counts + key, __popc(peers));
+    if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(cell_counts + key, __popc(peers));
+    const int blk = key >= 0 ? (key >> 6) : -1;
+    peers = __match_any_sync(0xffffffffu, blk);
+    if (blk >= 0 && lane == __ffs(peers) - 1) atomicAdd(counts + blk, __popc(peers));
 }
 
 // ---------------------------------------------------------------------------

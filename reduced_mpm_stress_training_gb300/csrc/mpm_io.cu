@@ -1,6 +1,7 @@
-// Data movement between the reference layout (AoS, user particle order) and
-// the internal sorted SoA state, the dense grid export, and the batched
-// element kernels (SVD, return map) used for unit-level checks.
+// Data movement between the reference layout (AoS vec3 / mat33 arrays in the
+// user's particle order) and the internal sorted particle records, the dense
+// grid export, and the batched element kernels (SVD, return map) used for
+// unit-level checks.
 #include "mpm_device.cuh"
 #include "mpm_launch.h"
 
@@ -15,18 +16,18 @@ int field_components(int field) {
     }
 }
 
-__device__ __forceinline__ float *field_ptr(const PState &st, int field) {
+// record word of component c of a field (see the record layout in mpm_device.cuh)
+__device__ __forceinline__ int field_word(int field, int c) {
     switch (field) {
-        case MPM_FIELD_X_INITIAL: return st.x0;
-        case MPM_FIELD_U: return st.u;
-        case MPM_FIELD_V: return st.v;
-        case MPM_FIELD_C: return st.C;
-        case MPM_FIELD_F: case MPM_FIELD_F_DISP: return st.F;
-        case MPM_FIELD_STRESS: return st.tau;
-        case MPM_FIELD_MASS: return st.mass;
-        case MPM_FIELD_VOL: return st.vol;
-        case MPM_FIELD_YIELD: return st.yld;
-        default: return st.u;  // MPM_FIELD_X reads u (plus x0)
+        case MPM_FIELD_X_INITIAL: case MPM_FIELD_X: return rec::X0 + c;
+        case MPM_FIELD_U: return rec::U + c;
+        case MPM_FIELD_V: return rec::V + c;
+        case MPM_FIELD_C: return rec::C + c;
+        case MPM_FIELD_STRESS: return rec::TAU + c;
+        case MPM_FIELD_F: case MPM_FIELD_F_DISP: return c < 8 ? rec::F0 + c : rec::F8;
+        case MPM_FIELD_MASS: return rec::MASS;
+        case MPM_FIELD_VOL: return rec::VOL;
+        default: return rec::YLD;  // MPM_FIELD_YIELD
     }
 }
 
@@ -35,15 +36,12 @@ __device__ __forceinline__ float *field_ptr(const PState &st, int field) {
 __global__ void init_state_kernel(PState a, PState b, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int64_t s = a.stride;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        float v = (k % 4 == 0) ? 1.0f : 0.0f;
-        a.F[i + k * s] = v;
-        b.F[i + k * s] = v;
-    }
-    a.uid[i] = i;
-    b.uid[i] = i;
+    float *ra = recw(a, i), *rb = recw(b, i);
+    for (int k = 0; k < kRecWords; ++k) { ra[k] = 0.0f; rb[k] = 0.0f; }
+    ra[rec::F0] = ra[rec::F0 + 4] = ra[rec::F8] = 1.0f;
+    rb[rec::F0] = rb[rec::F0 + 4] = rb[rec::F8] = 1.0f;
+    ra[rec::UID] = __int_as_float(i);
+    rb[rec::UID] = __int_as_float(i);
     a.key[i] = -1;
     b.key[i] = -1;
 }
@@ -51,19 +49,19 @@ __global__ void init_state_kernel(PState a, PState b, int n) {
 __global__ void load_kernel(PState st, int n, int field, int nc, const float *__restrict__ src) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int64_t u = st.uid[i];
-    float *dst = field_ptr(st, field);
-    for (int c = 0; c < nc; ++c) dst[i + c * st.stride] = src[u * nc + c];
+    float *r = recw(st, i);
+    const int64_t u = __float_as_int(r[rec::UID]);
+    for (int c = 0; c < nc; ++c) r[field_word(field, c)] = src[u * nc + c];
 }
 
 __global__ void export_kernel(PState st, int n, int field, int nc, float *__restrict__ dst) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int64_t u = st.uid[i];
-    const float *src = field_ptr(st, field);
+    const float *r = recw(st, i);
+    const int64_t u = __float_as_int(r[rec::UID]);
     for (int c = 0; c < nc; ++c) {
-        float v = src[i + c * st.stride];
-        if (field == MPM_FIELD_X) v = __fadd_rn(st.x0[i + c * st.stride], v);       // x0 + u (:5-7)
+        float v = r[field_word(field, c)];
+        if (field == MPM_FIELD_X) v = __fadd_rn(v, r[rec::U + c]);                 // x0 + u (:5-7)
         if (field == MPM_FIELD_F_DISP) v = v - ((c % 4 == 0) ? 1.0f : 0.0f);       // F - I (:16-19)
         dst[u * nc + c] = v;
     }

@@ -1,17 +1,20 @@
-// Per-substep particle ordering by 4x4x4 grid block ("bucket").
+// Per-substep particle ordering by grid cell, grouped by 4x4x4 grid block.
 //
 // The reference scatters every particle straight into global memory
 // (p2g_apic_stress_given, engine_stress/mpm_utils.py:190-227: 7 float
-// atomics per node, 189 per particle).  Here particles are grouped by the
-// grid block that holds their base cell, so P2G can accumulate a block's
-// nodes in shared memory.  The order is a single-digit counting (radix)
-// sort on the block key:
-//   keys + histogram  -- written by G2P for the next substep, or by
-//                        key_kernel after a load moved particles
-//   scan_tiles        -- per-tile sums of (count, chunks); the last CTA
-//                        to finish scans the tile sums (ticket, no spin)
-//   scan_finish       -- bucket offsets, cursors, the chunk work list
-//   scatter           -- order[] via warp-aggregated cursor atomics
+// atomics per node, 189 per particle).  Here particles are ordered by the
+// cell of their stencil base, block-major, so P2G can accumulate a block's
+// nodes in shared memory and find each cell's particles as one range.  The
+// order is a two-level counting (radix) sort on the cell key
+// block * 64 + cell:
+//   keys + histograms -- written by G2P for the next substep (block and
+//                        cell counts), or by key_kernel after a load moved
+//                        particles
+//   scan_tiles        -- per-tile sums of the block counts; the last CTA to
+//                        finish scans the tile sums (atomic ticket, no spin)
+//   scan_finish       -- block offsets, the P2G block list and the G2P chunk
+//                        list; for each non-empty block, its 64 cell offsets
+//   scatter           -- order[] via warp-aggregated cell-cursor atomics
 //   permute           -- every k substeps, physically reorder the state
 //                        so the order[] gathers stay coalesced
 #include "mpm_device.cuh"
@@ -25,16 +28,15 @@ __global__ void key_kernel(const MpmScene *__restrict__ scenes, int n_scenes, PS
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int key = -1;
     if (i < n) {
-        int uid = st.uid[i];
+        const float4 q0 = ldrec(st, i, 0), q1 = ldrec(st, i, 1), q2 = ldrec(st, i, 2);
+        const int uid = __float_as_int(q1.y);
         const MpmScene &S = scenes[scene_of_particle(scenes, n_scenes, uid)];
-        const int64_t sd = st.stride;
         bool ok;
-        key = particle_key(S, st.x0[i], st.x0[i + sd], st.x0[i + 2 * sd], st.u[i], st.u[i + sd],
-                           st.u[i + 2 * sd], ws.nbk - 1, ok);
+        key = particle_key(S, q0.x, q0.y, q0.z, q2.x, q2.y, q2.z, ws.nbk - 1, ok);
         if (!ok) atomicOr(status, MPM_ST_OUT_OF_DOMAIN);
         st.key[i] = key;
     }
-    warp_histogram(ws.counts, key);
+    warp_histogram(ws.counts, ws.cell_counts, key);
 }
 
 __device__ __forceinline__ int4 add4(int4 a, int4 b) {
@@ -143,9 +145,28 @@ __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__rest
     for (int j = 0; j < kScanPerThread; ++j) {
         int b = b0 + j;
         if (b >= ws.nbk) break;
-        ws.offsets[b] = off;
-        ws.cursor[b] = off;
         ws.counts[b] = 0;
+        // the out-of-domain bucket always gets its cursor: its particles are
+        // not re-counted by G2P, and they sort after every counted particle
+        if (cnt[j] > 0 || b == ws.nbk - 1) {
+            // cell offsets inside the block; zero its cell histogram
+            int4 *cc = reinterpret_cast<int4 *>(ws.cell_counts + (int64_t)b * 64);
+            int4 *cs4 = reinterpret_cast<int4 *>(ws.cell_start + (int64_t)b * 64);
+            int4 *cu4 = reinterpret_cast<int4 *>(ws.cell_cursor + (int64_t)b * 64);
+            int4 k[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) k[q] = cc[q];  // all loads in flight at once
+            int run = off;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int4 st4 = make_int4(run, run + k[q].x, run + k[q].x + k[q].y,
+                                           run + k[q].x + k[q].y + k[q].z);
+                run += k[q].x + k[q].y + k[q].z + k[q].w;
+                cs4[q] = st4;
+                cu4[q] = st4;
+                cc[q] = make_int4(0, 0, 0, 0);
+            }
+        }
         if (b < ws.nbk - 1 && cnt[j] > 0) {
             const int sc = scene_of_block(scenes, n_scenes, b);
             if (boff < ws.nbk - 1) ws.blocks[boff] = make_int4(b, off, cnt[j], sc);
@@ -164,7 +185,7 @@ __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__rest
     }
 }
 
-// order[cursor[key]++] = slot, warp-aggregated.  Also zeroes the grid
+// order[cell_cursor[key]++] = slot, warp-aggregated.  Also zeroes the grid
 // accumulator of the previous substep's active blocks (kept until now so
 // grid mass/momentum stay readable between substeps).
 __global__ void scatter_kernel(PState st, Ws ws, int n) {
@@ -177,34 +198,19 @@ __global__ void scatter_kernel(PState st, Ws ws, int n) {
     int lane = threadIdx.x & 31;
     int leader = __ffs(peers) - 1;
     int base = 0;
-    if (key >= 0 && lane == leader) base = atomicAdd(ws.cursor + key, __popc(peers));
+    if (key >= 0 && lane == leader) base = atomicAdd(ws.cell_cursor + key, __popc(peers));
     base = __shfl_sync(0xffffffffu, base, leader);
     const int pos = base + __popc(peers & ((1u << lane) - 1u));
     if (key >= 0 && pos < n) ws.order[pos] = i;
 }
 
-// physical re-sort: dst[i] = src[order[i]] for every field; order := identity
+// physical re-sort: dst[i] = src[order[i]] (whole records); order := identity
 __global__ void permute_kernel(PState src, PState dst, Ws ws, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int j = ws.order[i];
-    const int64_t s = src.stride;
+    const int j = ws.order[i];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        dst.x0[i + c * s] = src.x0[j + c * s];
-        dst.u[i + c * s] = src.u[j + c * s];
-        dst.v[i + c * s] = src.v[j + c * s];
-    }
-#pragma unroll
-    for (int c = 0; c < 9; ++c) {
-        dst.C[i + c * s] = src.C[j + c * s];
-        dst.F[i + c * s] = src.F[j + c * s];
-        dst.tau[i + c * s] = src.tau[j + c * s];
-    }
-    dst.mass[i] = src.mass[j];
-    dst.vol[i] = src.vol[j];
-    dst.yld[i] = src.yld[j];
-    dst.uid[i] = src.uid[j];
+    for (int q = 0; q < kRecQuads; ++q) strec(dst, i, q, ldrec(src, j, q));
     dst.key[i] = src.key[j];  // G2P rewrites all but the out-of-domain ones
     ws.order[i] = i;
 }

@@ -38,30 +38,24 @@ __device__ __forceinline__ void chunk_block(const MpmScene &S, int gblock, int &
 //   grid_v_in += (w m)(v + C dpos) + dt (-vol tau) grad w,  grid_m += w m
 //
 // One warp per non-empty grid block, with a warp-private 6x6x6 node tile in
-// shared memory and no floating-point atomics in the particle loop:
-//   (a) classify the block's particles by cell (64 cells), int shared atomics
-//       give each particle its rank within its cell;
-//   (b,c) counting sort by cell;
-//   (d) order "layer-major": layer r holds the r-th particle of every cell,
-//       so a window of 32 consecutive particles has (almost always) 32
-//       distinct cells, and their stencils hit distinct nodes for every node
-//       offset -- plain read-modify-writes of the tile are race-free;
-//   (e) per window, the rare lanes that share a cell (windows spanning two
-//       short layers) are serialised by __match_any_sync rank;
-//   flush: one float4 atomicAdd per non-zero tile node into the global grid.
-// Blocks with more than kPassCap particles are processed in passes.
+// shared memory and no floating-point atomics in the particle loop.  The
+// sort delivers the block's particles ordered by cell with each cell's range
+// (cell_start .. cell_cursor).  The warp walks them "layer-major": layer r
+// holds the r-th particle of every cell, so a window of 32 consecutive
+// entries has (almost always) 32 distinct cells, whose stencils hit distinct
+// nodes for every node offset -- plain read-modify-writes of the tile are
+// race-free.  The rare lanes that share a cell (windows spanning two short
+// layers) are serialised by __match_any_sync rank.  A window reads 32 whole
+// particle records (128 B each, float4 loads), so the scattered order costs
+// no extra DRAM sectors.  The tile is flushed with one float4 atomicAdd per
+// non-zero node into the global grid.
 // ---------------------------------------------------------------------------
 constexpr int kP2GWarps = 4;
-constexpr int kPassCap = 512;
+constexpr int kPassCap = 512;  // layer-major entries buffered per batch
 
 struct P2GWarpSmem {
     float4 tile[kTileNodes];
-    int cnt[64];
-    int cstart[64];
-    int sorted[kPassCap];
-    unsigned short perm[kPassCap];
-    unsigned short tmpr[kPassCap];
-    unsigned char tmpc[kPassCap];
+    int perm[kPassCap];  // sorted positions (indices into order[])
 };
 
 struct P2GParticle {
@@ -75,13 +69,17 @@ struct P2GParticle {
 
 __device__ __forceinline__ bool p2g_load(const MpmScene &S, const PState &st, int slot, int bx,
                                          int by, int bz, float dt, P2GParticle &P) {
-    const int64_t sd = st.stride;
+    // record quads 0-7: x0 m | vol .. | u v.x | v.yz C0 C1 | C2-5 | C6-8 tau0 | tau1-4 | tau5-8
+    const float4 q0 = ldrec(st, slot, 0), q1 = ldrec(st, slot, 1), q2 = ldrec(st, slot, 2),
+                 q3 = ldrec(st, slot, 3), q4 = ldrec(st, slot, 4), q5 = ldrec(st, slot, 5),
+                 q6 = ldrec(st, slot, 6), q7 = ldrec(st, slot, 7);
+    const float x0[3] = {q0.x, q0.y, q0.z}, u[3] = {q2.x, q2.y, q2.z};
     float gp[3];
     int base[3];
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        gp[d] = grid_coord(st.x0[slot + d * sd], st.u[slot + d * sd], S.inv_dx);
+        gp[d] = grid_coord(x0[d], u[d], S.inv_dx);
         ok &= stencil_base(gp[d], S.n_grid, base[d]);
     }
     P.lx = base[0] - 4 * bx;
@@ -90,19 +88,19 @@ __device__ __forceinline__ bool p2g_load(const MpmScene &S, const PState &st, in
     ok &= (unsigned)P.lx < 4u && (unsigned)P.ly < 4u && (unsigned)P.lz < 4u;
     if (!ok) return false;
     make_weights(gp, base, P.W);
-    P.m = st.mass[slot];
-    const float vol = st.vol[slot];
+    P.m = q0.w;
+    const float vol = q1.x;
     const float dx = S.dx;
-    float Cm[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) Cm[k] = st.C[slot + k * sd];
+    const float v[3] = {q2.w, q3.x, q3.y};
+    const float Cm[9] = {q3.z, q3.w, q4.x, q4.y, q4.z, q4.w, q5.x, q5.y, q5.z};
+    const float tau[9] = {q5.w, q6.x, q6.y, q6.z, q6.w, q7.x, q7.y, q7.z, q7.w};
     const float tscale = -vol * dt * S.inv_dx;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) P.T[k] = st.tau[slot + k * sd] * tscale;
+    for (int k = 0; k < 9; ++k) P.T[k] = tau[k] * tscale;
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
         const float cf = Cm[r * 3 + 0] * P.W.fx[0] + Cm[r * 3 + 1] * P.W.fx[1] + Cm[r * 3 + 2] * P.W.fx[2];
-        P.a0[r] = st.v[slot + r * sd] - cf * dx;
+        P.a0[r] = v[r] - cf * dx;
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) P.Cd[k] = Cm[k] * dx;
@@ -148,8 +146,8 @@ __device__ __forceinline__ void p2g_scatter(const P2GParticle &P, float4 *tile, 
 }
 
 __global__ void __launch_bounds__(kP2GWarps * 32, 4) p2g_kernel(const MpmScene *__restrict__ scenes,
-                                                             PState st, Ws ws, float dt,
-                                                             int *status) {
+                                                                PState st, Ws ws, float dt,
+                                                                int *status) {
     __shared__ P2GWarpSmem smem[kP2GWarps];
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -163,67 +161,37 @@ __global__ void __launch_bounds__(kP2GWarps * 32, 4) p2g_kernel(const MpmScene *
         int bx, by, bz;
         chunk_block(S, be.x, bx, by, bz);
         for (int i = lane; i < kTileNodes; i += 32) sm.tile[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int p0 = 0; p0 < be.z; p0 += kPassCap) {
-            const int np = min(kPassCap, be.z - p0);
-            sm.cnt[lane] = 0;
-            sm.cnt[lane + 32] = 0;
-            __syncwarp();
-            // (a) classify by cell
-            for (int i = lane; i < np; i += 32) {
-                const int idx = be.y + p0 + i;
-                int c = 255;
-                if (idx < ws.n) {
-                    const int slot = ws.order[idx];
-                    const int64_t sd = st.stride;
-                    int base[3];
-                    bool ok = true;
-#pragma unroll
-                    for (int d = 0; d < 3; ++d)
-                        ok &= stencil_base(grid_coord(st.x0[slot + d * sd], st.u[slot + d * sd], S.inv_dx),
-                                           S.n_grid, base[d]);
-                    const int lx = base[0] - 4 * bx, ly = base[1] - 4 * by, lz = base[2] - 4 * bz;
-                    ok &= (unsigned)lx < 4u && (unsigned)ly < 4u && (unsigned)lz < 4u;
-                    if (ok) c = (lx * 4 + ly) * 4 + lz;
-                    else atomicOr(status, MPM_ST_INTERNAL);
-                }
-                sm.tmpc[i] = (unsigned char)c;
-                if (c != 255) sm.tmpr[i] = (unsigned short)atomicAdd(&sm.cnt[c], 1);
-            }
-            __syncwarp();
-            // (b) cell offsets (exclusive scan over 64 cells, two per lane)
-            const int c0 = sm.cnt[lane], c1 = sm.cnt[lane + 32];
-            int s0 = c0, s1 = c1;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y0 = __shfl_up_sync(full, s0, o), y1 = __shfl_up_sync(full, s1, o);
-                if (lane >= o) { s0 += y0; s1 += y1; }
-            }
-            const int tot0 = __shfl_sync(full, s0, 31);
-            sm.cstart[lane] = s0 - c0;
-            sm.cstart[lane + 32] = tot0 + s1 - c1;
-            const int maxcnt = __reduce_max_sync(full, max(c0, c1));
-            __syncwarp();
-            // (c) cell-sorted slots
-            for (int i = lane; i < np; i += 32) {
-                const int c = sm.tmpc[i];
-                if (c != 255) sm.sorted[sm.cstart[c] + sm.tmpr[i]] = ws.order[be.y + p0 + i];
-            }
-            // (d) layer-major permutation
+        // cell ranges of this block: lane owns cells lane and lane + 32
+        const int64_t cb = (int64_t)be.x * 64;
+        const int s0 = ws.cell_start[cb + lane], s1 = ws.cell_start[cb + lane + 32];
+        const int c0 = max(0, ws.cell_cursor[cb + lane] - s0);
+        const int c1 = max(0, ws.cell_cursor[cb + lane + 32] - s1);
+        const int maxcnt = __reduce_max_sync(full, max(c0, c1));
+        int r = 0;
+        while (r < maxcnt) {
+            // layer-major batch: whole layers while they fit in the buffer
             int nv = 0;
-            for (int r = 0; r < maxcnt; ++r) {
+            while (r < maxcnt && nv <= kPassCap - 64) {
                 const bool a = c0 > r, b = c1 > r;
                 const unsigned ma = __ballot_sync(full, a), mb = __ballot_sync(full, b);
-                if (a) sm.perm[nv + __popc(ma & lt)] = (unsigned short)(sm.cstart[lane] + r);
-                if (b) sm.perm[nv + __popc(ma) + __popc(mb & lt)] = (unsigned short)(sm.cstart[lane + 32] + r);
+                if (a) sm.perm[nv + __popc(ma & lt)] = s0 + r;
+                if (b) sm.perm[nv + __popc(ma) + __popc(mb & lt)] = s1 + r;
                 nv += __popc(ma) + __popc(mb);
+                ++r;
             }
             __syncwarp();
-            // (e) windows of 32 particles
             for (int w0 = 0; w0 < nv; w0 += 32) {
                 const int k = w0 + lane;
                 bool act = k < nv;
                 P2GParticle P;
-                if (act) act = p2g_load(S, st, sm.sorted[sm.perm[k]], bx, by, bz, dt, P);
+                if (act) {
+                    const int idx = sm.perm[k];
+                    act = idx < ws.n;
+                    if (act) {
+                        act = p2g_load(S, st, ws.order[idx], bx, by, bz, dt, P);
+                        if (!act) atomicOr(status, MPM_ST_INTERNAL);
+                    }
+                }
                 const int cell = act ? (P.lx * 4 + P.ly) * 4 + P.lz : -1 - lane;
                 const unsigned peers = __match_any_sync(full, cell);
                 const int rank = act ? __popc(peers & lt) : 0;
@@ -319,13 +287,30 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
                                                  Ws ws, float dt, int *status) {
     __shared__ float4 tile[kTileNodes];
     const int n_chunks = *ws.n_chunks;
-    const int sentinel = ws.nbk - 1;
+    const int sentinel = (ws.nbk - 1) * 64;  // out-of-domain cell key
     for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         const int4 ch = ws.chunks[c];
         const MpmScene &S = scenes[ch.w];
         int bx, by, bz;
         chunk_block(S, ch.x, bx, by, bz);
         const int nb = S.n_blocks_axis;
+        // this thread's particle: issue its loads before the tile barrier
+        const bool mine = threadIdx.x < ch.z && ch.y + (int)threadIdx.x < ws.n;
+        const int slot = mine ? ws.order[ch.y + threadIdx.x] : 0;
+        float x0[3], xo[3], Fp[9];
+        float4 q1 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (mine) {
+            // record quads 0 (x0), 1 (vol uid yield F8), 2 (u), 8-9 (F0-7)
+            const float4 q0 = ldrec(st, slot, 0), q2 = ldrec(st, slot, 2), q8 = ldrec(st, slot, 8),
+                         q9 = ldrec(st, slot, 9);
+            q1 = ldrec(st, slot, 1);
+            x0[0] = q0.x; x0[1] = q0.y; x0[2] = q0.z;
+            xo[0] = __fadd_rn(x0[0], q2.x);
+            xo[1] = __fadd_rn(x0[1], q2.y);
+            xo[2] = __fadd_rn(x0[2], q2.z);
+            Fp[0] = q8.x; Fp[1] = q8.y; Fp[2] = q8.z; Fp[3] = q8.w;
+            Fp[4] = q9.x; Fp[5] = q9.y; Fp[6] = q9.z; Fp[7] = q9.w; Fp[8] = q1.w;
+        }
         for (int i = threadIdx.x; i < kTileNodes; i += CH) {
             const int tx = i / 36, ty = (i / 6) % 6, tz = i % 6;
             const int ix = 4 * bx + tx, iy = 4 * by + ty, iz = 4 * bz + tz;
@@ -336,16 +321,12 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
         }
         __syncthreads();
         int key = -1;
-        if (threadIdx.x < ch.z && ch.y + (int)threadIdx.x < ws.n) {
-            const int slot = ws.order[ch.y + threadIdx.x];
-            const int64_t sd = st.stride;
-            float x0[3], gp[3], xo[3];
+        if (mine) {
+            float gp[3];
             int base[3];
             bool ok = true;
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                x0[d] = st.x0[slot + d * sd];
-                xo[d] = __fadd_rn(x0[d], st.u[slot + d * sd]);
                 gp[d] = __fmul_rn(xo[d], S.inv_dx);
                 ok &= stencil_base(gp[d], S.n_grid, base[d]);
             }
@@ -421,9 +402,7 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
                     un[d] = __fsub_rn(xn, x0[d]);
                 }
                 // F_trial = (I + dt grad v) F (:281)
-                float Fp[9], A[9], Ft[9];
-#pragma unroll
-                for (int k = 0; k < 9; ++k) Fp[k] = st.F[slot + k * sd];
+                float A[9], Ft[9];
 #pragma unroll
                 for (int k = 0; k < 9; ++k) A[k] = ((k % 4 == 0) ? 1.0f : 0.0f) + nF[k] * dt;
 #pragma unroll
@@ -432,36 +411,35 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
                     for (int q = 0; q < 3; ++q)
                         Ft[r * 3 + q] = A[r * 3 + 0] * Fp[0 * 3 + q] + A[r * 3 + 1] * Fp[1 * 3 + q] +
                                         A[r * 3 + 2] * Fp[2 * 3 + q];
-                float yld = (S.material == MPM_METAL) ? st.yld[slot] : 0.0f;
+                float yld = (S.material == MPM_METAL) ? q1.z : 0.0f;
                 float Fo[9], tau[9];
                 return_map_stress(S, Ft, yld, Fo, tau);
-                // stores
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    st.v[slot + d * sd] = nv[d];
-                    st.u[slot + d * sd] = un[d];
-                }
+                // stores: record quads 1-9
                 float chk = 0.0f;
 #pragma unroll
-                for (int k = 0; k < 9; ++k) {
-                    st.C[slot + k * sd] = nC[k];
-                    st.F[slot + k * sd] = Fo[k];
-                    st.tau[slot + k * sd] = tau[k];
-                    chk += fabsf(Fo[k]) + fabsf(tau[k]);
-                }
-                if (S.material == MPM_METAL && S.hardening == 1) st.yld[slot] = yld;
+                for (int k = 0; k < 9; ++k) chk += fabsf(Fo[k]) + fabsf(tau[k]);
+                if (!(S.material == MPM_METAL && S.hardening == 1)) yld = q1.z;
+                strec(st, slot, 1, make_float4(q1.x, q1.y, yld, Fo[8]));
+                strec(st, slot, 2, make_float4(un[0], un[1], un[2], nv[0]));
+                strec(st, slot, 3, make_float4(nv[1], nv[2], nC[0], nC[1]));
+                strec(st, slot, 4, make_float4(nC[2], nC[3], nC[4], nC[5]));
+                strec(st, slot, 5, make_float4(nC[6], nC[7], nC[8], tau[0]));
+                strec(st, slot, 6, make_float4(tau[1], tau[2], tau[3], tau[4]));
+                strec(st, slot, 7, make_float4(tau[5], tau[6], tau[7], tau[8]));
+                strec(st, slot, 8, make_float4(Fo[0], Fo[1], Fo[2], Fo[3]));
+                strec(st, slot, 9, make_float4(Fo[4], Fo[5], Fo[6], Fo[7]));
                 int flags = 0;
                 const float vmax = S.dx / dt;
                 if (fabsf(nv[0]) > vmax || fabsf(nv[1]) > vmax || fabsf(nv[2]) > vmax) flags |= MPM_ST_CFL;
                 if (!isfinite(chk)) flags |= MPM_ST_NONFINITE;
                 bool kok;
-                key = particle_key(S, x0[0], x0[1], x0[2], un[0], un[1], un[2], sentinel, kok);
+                key = particle_key(S, x0[0], x0[1], x0[2], un[0], un[1], un[2], ws.nbk - 1, kok);
                 if (!kok) flags |= MPM_ST_OUT_OF_DOMAIN;
                 if (flags) atomicOr(status, flags);
                 st.key[slot] = key;
             }
         }
-        warp_histogram(ws.counts, key);
+        warp_histogram(ws.counts, ws.cell_counts, key);
         __syncthreads();
     }
 }
@@ -478,9 +456,9 @@ static int persistent_grid(const Ctx &cx, int per_sm) {
 }
 
 cudaError_t launch_p2g(const Ctx &cx, float dt) {
-    // persistent: enough warps to fill every SM, never more than the blocks
+    // persistent: four CTAs (16 warps) per SM, never more warps than blocks
     int64_t want = (cx.total_blocks + kP2GWarps - 1) / kP2GWarps;
-    int grid = (int)(want < (int64_t)cx.num_sms * 6 ? want : (int64_t)cx.num_sms * 6);
+    int grid = (int)(want < (int64_t)cx.num_sms * 4 ? want : (int64_t)cx.num_sms * 4);
     if (grid < 1) grid = 1;
     p2g_kernel<<<grid, kP2GWarps * 32, 0, cx.stream>>>(cx.scenes, cx.st, cx.ws, dt, cx.status);
     return cudaGetLastError();
