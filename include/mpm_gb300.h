@@ -192,6 +192,20 @@ int mpm_g2p(MpmBuffers *b, float dt, void *stream); /* mpm_utils.py:241-306, :4-
 int mpm_export_grid(MpmBuffers *b, int32_t scene, float *grid_m, float *grid_v_in,
                     float *grid_v_out, void *stream);
 
+/* No counterpart in the reference (its Warp launches always use arrays the
+ * simulator allocated).  The substep of mpm_p2g2p for callers that cannot
+ * allocate device memory -- e.g. a host framework that has reserved nearly all
+ * device memory for its own pool, or code that runs where cudaMalloc is not
+ * allowed: b->workspace is ignored (may be NULL) and the scratch lives in one
+ * library-owned 16 MiB device array (held by every GPU that loads the
+ * library).  Returns MPM_ERR_SIZE if b->plan.workspace_bytes exceeds 16 MiB
+ * (a 64^3 grid with 32,768 particles fits).  All calls share that array: each
+ * call clears it and re-sorts from the particle positions, and calls that
+ * overlap on the GPU race.  The first call on a device looks up the array's
+ * address (cudaGetSymbolAddress); make it before any stream capture.  Never
+ * allocates. */
+int mpm_p2g2p_noalloc(MpmBuffers *b, float time, float dt, void *stream);
+
 /* ---- element kernels on plain arrays --------------------------------- */
 
 /* Batched 3x3 SVD, A (n,9) row-major -> U (n,9), s (n,3), V (n,9):
