@@ -229,8 +229,7 @@ def gb300_arm(args, sc, world, rank, local):
 
     device = torch.device(f"cuda:{local}")
     torch.cuda.set_device(device)
-    resort = 16
-    sim = build_simulator(sc, device=device, resort_interval=resort)
+    sim = build_simulator(sc, device=device)
     eng = sim._engine
     n = sc.n_particles
     dt = sc.dt
@@ -240,7 +239,7 @@ def gb300_arm(args, sc, world, rank, local):
     torch.cuda.synchronize()
     sim.check_status()
 
-    gsize = 2 * resort
+    gsize = 32
     graph = eng.graph(gsize, float(sim.time), dt)
     torch.cuda.synchronize()
     st = torch.cuda.current_stream()
@@ -262,7 +261,7 @@ def gb300_arm(args, sc, world, rank, local):
     t = ev0.elapsed_time(ev1) / 1e3
     t_max = max_over_ranks(t, world, device)
     status = eng.status()
-    launches_per_substep = 6 + 1.0 / resort  # 3 sort + p2g + grid + g2p (+ periodic re-sort)
+    launches_per_substep = 6  # scan_tiles, scan_finish, scatter, p2g, grid, g2p
     value = world * n * K / t_max
     ms_per_step = 1e3 * t_max / K
 

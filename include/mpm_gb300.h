@@ -106,10 +106,11 @@ typedef struct MpmBuffers {
     void *scenes;     /* device copy of the MpmScene table (mpm_upload_scenes)  */
     int32_t *status;  /* one device int32, MPM_ST_* bits, OR-accumulated        */
     MpmPlan plan;
-    int32_t cur;             /* index of the live state buffer                  */
+    int32_t cur;             /* index of the live state buffer; every substep
+                                flips it (G2P writes the updated records, sorted
+                                by cell, into the other buffer)                 */
     int32_t keys_valid;      /* 0 after a load that moves particles             */
-    int32_t resort_interval; /* physical re-sort every k substeps (0: only when
-                                keys were invalid)                              */
+    int32_t reserved0;
     int32_t pad0;
     int64_t substep;         /* substeps taken since mpm_init                   */
 } MpmBuffers;

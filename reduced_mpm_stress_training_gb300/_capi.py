@@ -54,7 +54,7 @@ class MpmPlan(C.Structure):
 class MpmBuffers(C.Structure):
     _fields_ = [("state", C.c_void_p * 2), ("workspace", C.c_void_p), ("scenes", C.c_void_p),
                 ("status", C.c_void_p), ("plan", MpmPlan), ("cur", C.c_int32),
-                ("keys_valid", C.c_int32), ("resort_interval", C.c_int32), ("pad0", C.c_int32),
+                ("keys_valid", C.c_int32), ("reserved0", C.c_int32), ("pad0", C.c_int32),
                 ("substep", C.c_int64)]
 
 

@@ -92,6 +92,7 @@ mpm::Ctx make_ctx(const MpmBuffers *b, void *stream, int which) {
     cx.scenes = static_cast<const MpmScene *>(b->scenes);
     cx.n_scenes = p.n_scenes;
     cx.st = state_view(b->state[which], p.particle_stride);
+    cx.st2 = state_view(b->state[which ^ 1], p.particle_stride);
     mpm::Ws &ws = cx.ws;
     ws.order = reinterpret_cast<int *>(w + L.order);
     ws.counts = reinterpret_cast<int *>(w + L.counts);
@@ -184,7 +185,8 @@ int mpm_plan(MpmScene *scenes, int32_t n_scenes, int64_t n_particles, int32_t ch
     p.chunk_size = chunk_size;
     p.n_scenes = n_scenes;
     const int64_t nonempty = n_particles < blocks ? n_particles : blocks;
-    p.max_chunks = n_particles / chunk_size + nonempty + 1;
+    // G2P chunks of the blocks, plus the out-of-domain copy chunks
+    p.max_chunks = 2 * (n_particles / chunk_size) + nonempty + 2;
     p.state_bytes = kStateBytesPerParticle * p.particle_stride;
     p.workspace_bytes = ws_layout(p).total;
     *plan = p;
@@ -248,21 +250,13 @@ int mpm_export(MpmBuffers *b, int32_t field, float *dst, int32_t dst_on_host, vo
 int mpm_sort(MpmBuffers *b, void *stream) {
     if (!buffers_ok(b)) return MPM_ERR_ARG;
     mpm::Ctx cx = make_ctx(b, stream, b->cur);
-    bool resort = false;
     if (!b->keys_valid) {
         MPM_CHECK(cudaMemsetAsync(cx.ws.counts, 0, (size_t)cx.ws.nbk * sizeof(int), cx.stream));
         MPM_CHECK(cudaMemsetAsync(cx.ws.cell_counts, 0, (size_t)cx.ws.nbk * 64 * sizeof(int), cx.stream));
         MPM_CHECK(mpm::launch_keys(cx));
         b->keys_valid = 1;
-        resort = true;
     }
     MPM_CHECK(mpm::launch_sort(cx));
-    if (b->resort_interval > 0 && b->substep % b->resort_interval == 0) resort = true;
-    if (resort) {
-        mpm::PState dst = state_view(b->state[b->cur ^ 1], b->plan.particle_stride);
-        MPM_CHECK(mpm::launch_permute(cx, dst));
-        b->cur ^= 1;
-    }
     return MPM_OK;
 }
 
@@ -281,6 +275,7 @@ int mpm_grid_update(MpmBuffers *b, float time, float dt, void *stream) {
 int mpm_g2p(MpmBuffers *b, float dt, void *stream) {
     if (!buffers_ok(b)) return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_g2p(make_ctx(b, stream, b->cur), dt));
+    b->cur ^= 1;  // G2P wrote the sorted, updated records into the other buffer
     b->substep += 1;
     return MPM_OK;
 }

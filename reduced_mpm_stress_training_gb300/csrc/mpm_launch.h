@@ -12,6 +12,7 @@ struct Ctx {
     const MpmScene *scenes;  // device scene table
     int n_scenes;
     PState st;               // live state buffer
+    PState st2;              // the other state buffer (G2P writes the sorted records there)
     Ws ws;
     int n;                   // particles
     int *status;
@@ -23,7 +24,6 @@ struct Ctx {
 // sort stage (mpm_sort.cu)
 cudaError_t launch_keys(const Ctx &cx);
 cudaError_t launch_sort(const Ctx &cx);
-cudaError_t launch_permute(const Ctx &cx, const PState &dst);
 
 // transfer stages (mpm_substep.cu)
 cudaError_t launch_p2g(const Ctx &cx, float dt);

@@ -15,8 +15,9 @@
 //   scan_finish       -- block offsets, the P2G block list and the G2P chunk
 //                        list; for each non-empty block, its 64 cell offsets
 //   scatter           -- order[] via warp-aggregated cell-cursor atomics
-//   permute           -- every k substeps, physically reorder the state
-//                        so the order[] gathers stay coalesced
+// G2P then writes every record to the other state buffer at its sorted
+// position, so order[] stays close to the identity from one substep to the
+// next and the gathers through it stay coalesced.
 #include "mpm_device.cuh"
 #include "mpm_launch.h"
 
@@ -68,11 +69,12 @@ __device__ __forceinline__ int4 cta_scan4(int4 v, int4 *wsum /* [8] shared */, i
     return add4(pre, x);
 }
 
-// per-bucket triple: (particles, G2P chunks, non-empty) -- the sentinel
-// bucket (out-of-domain particles) contributes particles only
+// per-bucket triple: (particles, G2P chunks, non-empty blocks) -- the
+// sentinel bucket (out-of-domain particles) gets copy chunks but no block
 __device__ __forceinline__ int4 bucket_triple(const Ws &ws, int b, int cnt) {
-    if (b >= ws.nbk - 1) return make_int4(cnt, 0, 0, 0);
-    return make_int4(cnt, (cnt + ws.chunk_size - 1) / ws.chunk_size, cnt > 0 ? 1 : 0, 0);
+    const int ch = (cnt + ws.chunk_size - 1) / ws.chunk_size;
+    if (b >= ws.nbk - 1) return make_int4(cnt, ch, 0, 0);
+    return make_int4(cnt, ch, cnt > 0 ? 1 : 0, 0);
 }
 
 // Phase 1: per-tile sums.  The last CTA to finish (atomic ticket; nobody
@@ -167,10 +169,13 @@ __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__rest
                 cc[q] = make_int4(0, 0, 0, 0);
             }
         }
-        if (b < ws.nbk - 1 && cnt[j] > 0) {
-            const int sc = scene_of_block(scenes, n_scenes, b);
-            if (boff < ws.nbk - 1) ws.blocks[boff] = make_int4(b, off, cnt[j], sc);
-            ++boff;
+        if (cnt[j] > 0) {
+            const bool real = b < ws.nbk - 1;
+            const int sc = real ? scene_of_block(scenes, n_scenes, b) : -1;  // -1: copy chunk
+            if (real) {
+                if (boff < ws.nbk - 1) ws.blocks[boff] = make_int4(b, off, cnt[j], sc);
+                ++boff;
+            }
             for (int s = 0; s < cnt[j]; s += cs) {
                 if (coff < ws.max_chunks)
                     ws.chunks[coff] = make_int4(b, off + s, min(cs, cnt[j] - s), sc);
@@ -204,17 +209,6 @@ __global__ void scatter_kernel(PState st, Ws ws, int n) {
     if (key >= 0 && pos < n) ws.order[pos] = i;
 }
 
-// physical re-sort: dst[i] = src[order[i]] (whole records); order := identity
-__global__ void permute_kernel(PState src, PState dst, Ws ws, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int j = ws.order[i];
-#pragma unroll
-    for (int q = 0; q < kRecQuads; ++q) strec(dst, i, q, ldrec(src, j, q));
-    dst.key[i] = src.key[j];  // G2P rewrites all but the out-of-domain ones
-    ws.order[i] = i;
-}
-
 cudaError_t launch_keys(const Ctx &cx) {
     if (cx.n == 0) return cudaSuccess;
     key_kernel<<<(cx.n + 255) / 256, 256, 0, cx.stream>>>(cx.scenes, cx.n_scenes, cx.st, cx.ws,
@@ -230,10 +224,5 @@ cudaError_t launch_sort(const Ctx &cx) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_permute(const Ctx &cx, const PState &dst) {
-    if (cx.n == 0) return cudaSuccess;
-    permute_kernel<<<(cx.n + 255) / 256, 256, 0, cx.stream>>>(cx.st, dst, cx.ws, cx.n);
-    return cudaGetLastError();
-}
 
 }  // namespace mpm

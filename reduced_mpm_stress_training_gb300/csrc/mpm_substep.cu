@@ -17,8 +17,10 @@
 //   g2p  -- one CTA per chunk: stage the tile of grid velocities in shared
 //           memory, gather 27 nodes per particle, APIC C, velocity
 //           gradient, F update, return map + stress on one SVD, the
-//           displacement update and the block key + histogram of the next
-//           substep.
+//           displacement update and the cell key + histograms of the next
+//           substep.  Each updated record is written to the other state
+//           buffer at its sorted position, so every substep leaves the
+//           particle state physically sorted by cell.
 #include "mpm_device.cuh"
 #include "mpm_launch.h"
 
@@ -281,28 +283,40 @@ __global__ void __launch_bounds__(256) grid_kernel(const MpmScene *__restrict__ 
 // ---------------------------------------------------------------------------
 // G2P: g2p_apic_and_stress (engine_stress/mpm_utils.py:241-306) fused with
 // update_x_from_u / update_u_from_x (:4-15) and the next substep's key.
+// Reads records from `st` through order[], writes them to `out` at the
+// sorted position.  Chunks with scene -1 hold out-of-domain particles,
+// which are carried over unchanged.
 // ---------------------------------------------------------------------------
 template <int CH>
 __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ scenes, PState st,
-                                                 Ws ws, float dt, int *status) {
+                                                 PState out, Ws ws, float dt, int *status) {
     __shared__ float4 tile[kTileNodes];
     const int n_chunks = *ws.n_chunks;
     const int sentinel = (ws.nbk - 1) * 64;  // out-of-domain cell key
     for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         const int4 ch = ws.chunks[c];
+        const int pos = ch.y + (int)threadIdx.x;  // sorted position of this thread's particle
+        const bool mine = (int)threadIdx.x < ch.z && pos < ws.n;
+        const int slot = mine ? ws.order[pos] : 0;
+        if (ch.w < 0) {  // out-of-domain particles: carry the records over (uniform per CTA)
+            if (mine) {
+#pragma unroll
+                for (int q = 0; q < kRecQuads; ++q) strec(out, pos, q, ldrec(st, slot, q));
+                out.key[pos] = st.key[slot];
+            }
+            continue;
+        }
         const MpmScene &S = scenes[ch.w];
         int bx, by, bz;
         chunk_block(S, ch.x, bx, by, bz);
         const int nb = S.n_blocks_axis;
         // this thread's particle: issue its loads before the tile barrier
-        const bool mine = threadIdx.x < ch.z && ch.y + (int)threadIdx.x < ws.n;
-        const int slot = mine ? ws.order[ch.y + threadIdx.x] : 0;
         float x0[3], xo[3], Fp[9];
-        float4 q1 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
         if (mine) {
-            // record quads 0 (x0), 1 (vol uid yield F8), 2 (u), 8-9 (F0-7)
-            const float4 q0 = ldrec(st, slot, 0), q2 = ldrec(st, slot, 2), q8 = ldrec(st, slot, 8),
-                         q9 = ldrec(st, slot, 9);
+            // record quads 0 (x0 m), 1 (vol uid yield F8), 2 (u), 8-9 (F0-7)
+            const float4 q2 = ldrec(st, slot, 2), q8 = ldrec(st, slot, 8), q9 = ldrec(st, slot, 9);
+            q0 = ldrec(st, slot, 0);
             q1 = ldrec(st, slot, 1);
             x0[0] = q0.x; x0[1] = q0.y; x0[2] = q0.z;
             xo[0] = __fadd_rn(x0[0], q2.x);
@@ -335,7 +349,9 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
             if (!ok) {
                 atomicOr(status, MPM_ST_INTERNAL);
                 key = sentinel;
-                st.key[slot] = key;
+#pragma unroll
+                for (int q = 0; q < kRecQuads; ++q) strec(out, pos, q, ldrec(st, slot, q));
+                out.key[pos] = key;
             } else {
                 Weights W;
                 make_weights(gp, base, W);
@@ -419,15 +435,16 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
 #pragma unroll
                 for (int k = 0; k < 9; ++k) chk += fabsf(Fo[k]) + fabsf(tau[k]);
                 if (!(S.material == MPM_METAL && S.hardening == 1)) yld = q1.z;
-                strec(st, slot, 1, make_float4(q1.x, q1.y, yld, Fo[8]));
-                strec(st, slot, 2, make_float4(un[0], un[1], un[2], nv[0]));
-                strec(st, slot, 3, make_float4(nv[1], nv[2], nC[0], nC[1]));
-                strec(st, slot, 4, make_float4(nC[2], nC[3], nC[4], nC[5]));
-                strec(st, slot, 5, make_float4(nC[6], nC[7], nC[8], tau[0]));
-                strec(st, slot, 6, make_float4(tau[1], tau[2], tau[3], tau[4]));
-                strec(st, slot, 7, make_float4(tau[5], tau[6], tau[7], tau[8]));
-                strec(st, slot, 8, make_float4(Fo[0], Fo[1], Fo[2], Fo[3]));
-                strec(st, slot, 9, make_float4(Fo[4], Fo[5], Fo[6], Fo[7]));
+                strec(out, pos, 0, q0);
+                strec(out, pos, 1, make_float4(q1.x, q1.y, yld, Fo[8]));
+                strec(out, pos, 2, make_float4(un[0], un[1], un[2], nv[0]));
+                strec(out, pos, 3, make_float4(nv[1], nv[2], nC[0], nC[1]));
+                strec(out, pos, 4, make_float4(nC[2], nC[3], nC[4], nC[5]));
+                strec(out, pos, 5, make_float4(nC[6], nC[7], nC[8], tau[0]));
+                strec(out, pos, 6, make_float4(tau[1], tau[2], tau[3], tau[4]));
+                strec(out, pos, 7, make_float4(tau[5], tau[6], tau[7], tau[8]));
+                strec(out, pos, 8, make_float4(Fo[0], Fo[1], Fo[2], Fo[3]));
+                strec(out, pos, 9, make_float4(Fo[4], Fo[5], Fo[6], Fo[7]));
                 int flags = 0;
                 const float vmax = S.dx / dt;
                 if (fabsf(nv[0]) > vmax || fabsf(nv[1]) > vmax || fabsf(nv[2]) > vmax) flags |= MPM_ST_CFL;
@@ -436,7 +453,7 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
                 key = particle_key(S, x0[0], x0[1], x0[2], un[0], un[1], un[2], ws.nbk - 1, kok);
                 if (!kok) flags |= MPM_ST_OUT_OF_DOMAIN;
                 if (flags) atomicOr(status, flags);
-                st.key[slot] = key;
+                out.key[pos] = key;
             }
         }
         warp_histogram(ws.counts, ws.cell_counts, key);
@@ -446,7 +463,7 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
 
 template <int CH>
 static cudaError_t g2p_t(const Ctx &cx, float dt, int grid) {
-    g2p_kernel<CH><<<grid, CH, 0, cx.stream>>>(cx.scenes, cx.st, cx.ws, dt, cx.status);
+    g2p_kernel<CH><<<grid, CH, 0, cx.stream>>>(cx.scenes, cx.st, cx.st2, cx.ws, dt, cx.status);
     return cudaGetLastError();
 }
 

@@ -146,15 +146,13 @@ def _stream_handle(device: torch.device) -> int:
 class MPMEngine:
     """Device buffers + C-ABI driver for one or more scenes (concatenated)."""
 
-    def __init__(self, scenes: list[SceneParams], device="cuda:0", chunk_size: int = 128,
-                 resort_interval: int = 16):
+    def __init__(self, scenes: list[SceneParams], device="cuda:0", chunk_size: int = 128):
         self.lib = A.load()
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise ValueError("MPMEngine runs on a CUDA device only (no CPU path)")
         self.scenes = list(scenes)
         self.chunk_size = chunk_size
-        self.resort_interval = resort_interval
         self.on_error = "raise"
         self._pending = None
         self._allocate(fresh=True)
@@ -198,7 +196,6 @@ class MPMEngine:
         b.scenes = self._scenes_dev.data_ptr()
         b.status = self._status.data_ptr()
         b.plan = plan
-        b.resort_interval = self.resort_interval
         self.buf = b
         self._upload()
         if fresh:
@@ -332,10 +329,9 @@ class SubstepGraph:
 
     The library's host-side control (live state buffer, substep counter) moves
     as the substeps are recorded; a replay runs the recorded launches with the
-    recorded buffer pointers.  So n must contain an even number of physical
-    re-sorts (n a multiple of 2 * resort_interval, or resort_interval 0) and
-    the block keys must be valid when capturing (take one eager substep
-    first).  ``time`` is frozen at capture: colliders with finite time windows
+    recorded buffer pointers.  Every substep flips the live state buffer, so
+    n must be even, and the block keys must be valid when capturing (take one
+    eager substep first).  ``time`` is frozen at capture: colliders with finite time windows
     need eager stepping.  The status word is not read inside the graph; call
     ``engine.status()`` after replays.
     """
@@ -356,8 +352,7 @@ class SubstepGraph:
         if b.cur != cur0:
             b.cur = cur0
             b.substep = step0
-            raise ValueError("a captured window must contain an even number of re-sorts: "
-                             "use n a multiple of 2 * resort_interval")
+            raise ValueError("a captured window must hold an even number of substeps")
         b.substep = step0  # nothing has run yet
 
     def replay(self) -> None:

@@ -148,7 +148,7 @@ SCENES = {
 }
 
 
-def build_simulator(sc: Scene, device="cuda:0", chunk_size: int = 128, resort_interval: int = 16):
+def build_simulator(sc: Scene, device="cuda:0", chunk_size: int = 128):
     """An MPM_Simulator_WARP loaded with the scene (particles, material, colliders)."""
     import torch
 
@@ -156,7 +156,7 @@ def build_simulator(sc: Scene, device="cuda:0", chunk_size: int = 128, resort_in
 
     x0, v0, vol, mass = sc.particles()
     sim = MPM_Simulator_WARP(sc.n_particles, n_grid=sc.n_grid, grid_lim=sc.grid_lim, device=device,
-                             chunk_size=chunk_size, resort_interval=resort_interval)
+                             chunk_size=chunk_size)
     sim.set_parameters(material=sc.material, E=sc.E, nu=sc.nu, friction_angle=sc.friction_angle,
                        gravity=sc.gravity, hardening=sc.hardening, xi=sc.xi)
     if sc.material == "metal":

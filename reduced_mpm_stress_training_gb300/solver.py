@@ -88,9 +88,8 @@ class MPMSimulator:
     """GB300 replacement of MPM_Simulator_WARP (engine_stress/mpm_solver_warp.py:24)."""
 
     def __init__(self, n_particles, n_grid=100, grid_lim=1.0, device="cuda:0", *,
-                 chunk_size: int = 128, resort_interval: int = 16):
+                 chunk_size: int = 128):
         self._chunk_size = chunk_size
-        self._resort_interval = resort_interval
         self.initialize(n_particles, n_grid, grid_lim, device=device)
 
     # --------------------------------------------------------------- set-up
@@ -102,8 +101,7 @@ class MPMSimulator:
                                    grid_lim=float(grid_lim), material=A.JELLY, mu=mu, lam=lam,
                                    friction_angle=25.0, gravity=(0.0, 0.0, 0.0))
         self._E, self._nu = 1000.0, 0.3
-        self._engine = MPMEngine([self._params], device=device, chunk_size=self._chunk_size,
-                                 resort_interval=self._resort_interval)
+        self._engine = MPMEngine([self._params], device=device, chunk_size=self._chunk_size)
         self.device = self._engine.device
         self._density = torch.zeros(self.n_particles, dtype=torch.float32, device=self.device)
         self._f_disp_loaded = None

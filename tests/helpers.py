@@ -16,13 +16,12 @@ def rel(a, b) -> float:
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-def gpu_sim(sc: S.Scene, device="cuda:0", chunk_size=128, resort_interval=16, x0=None, v0=None,
+def gpu_sim(sc: S.Scene, device="cuda:0", chunk_size=128, x0=None, v0=None,
             vol=None, mass=None, colliders=True):
     if x0 is None:
         x0, v0, vol, mass = sc.particles()
     sim = MPM_Simulator_WARP(sc.n_particles, n_grid=sc.n_grid, grid_lim=sc.grid_lim,
-                             device=device, chunk_size=chunk_size,
-                             resort_interval=resort_interval)
+                             device=device, chunk_size=chunk_size)
     sim.set_parameters(material=sc.material, E=sc.E, nu=sc.nu,
                        friction_angle=sc.friction_angle, gravity=sc.gravity,
                        hardening=sc.hardening, xi=sc.xi)
