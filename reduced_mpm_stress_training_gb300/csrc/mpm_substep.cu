@@ -286,56 +286,119 @@ __global__ void __launch_bounds__(256) grid_kernel(const MpmScene *__restrict__ 
 // Reads records from `st` through order[], writes them to `out` at the
 // sorted position.  Chunks with scene -1 hold out-of-domain particles,
 // which are carried over unchanged.
+//
+// Software-pipelined over the CTA's chunks: while chunk k is computed, the
+// particle records (quads 0,1,2,8,9) and the 6x6x6 grid-velocity tile of
+// chunk k+1 stream into the other half of a double buffer in shared memory
+// with cp.async, and the order[] indices of chunk k+2 are loaded.  The
+// updated records are assembled in shared memory and written to their
+// (contiguous) sorted range with coalesced float4 stores.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+constexpr int kG2PQuads = 5;  // record quads G2P reads: 0, 1, 2, 8, 9
+__device__ __forceinline__ int g2p_quad(int q) { return q < 3 ? q : q + 5; }
+
+constexpr int kOutStride = kRecQuads + 1;  // padded so the per-thread record writes are conflict-free
+
+template <int CH>
+struct G2PSmem {
+    float4 tile[2][kTileNodes];
+    float4 rec[2][kG2PQuads][CH];
+    float4 outrec[CH * kOutStride];  // updated records of the chunk, written out coalesced
+};
+
+// queue the async copies of one chunk into buffer b
+template <int CH>
+__device__ __forceinline__ void g2p_prefetch(const MpmScene *__restrict__ scenes, const PState &st,
+                                             const Ws &ws, const int4 &ch, int slot,
+                                             G2PSmem<CH> &sm, int b) {
+    if (ch.w < 0) return;  // copy chunk: no compute, nothing to stage
+    if ((int)threadIdx.x < ch.z && ch.y + (int)threadIdx.x < ws.n) {
+#pragma unroll
+        for (int q = 0; q < kG2PQuads; ++q)
+            cp_async16(&sm.rec[b][q][threadIdx.x], st.rec + (int64_t)slot * kRecQuads + g2p_quad(q), 16);
+    }
+    const MpmScene &S = scenes[ch.w];
+    int bx, by, bz;
+    chunk_block(S, ch.x, bx, by, bz);
+    const int nb = S.n_blocks_axis;
+    for (int i = threadIdx.x; i < kTileNodes; i += CH) {
+        const int tx = i / 36, ty = (i / 6) % 6, tz = i % 6;
+        const int ix = 4 * bx + tx, iy = 4 * by + ty, iz = 4 * bz + tz;
+        const bool in = ix < S.n_grid && iy < S.n_grid && iz < S.n_grid;
+        const float4 *src = ws.grid_v + (in ? node_addr(S.block_begin, nb, ix, iy, iz) : 0);
+        cp_async16(&sm.tile[b][i], src, in ? 16 : 0);  // outside the grid: zero fill
+    }
+}
+
+__device__ __forceinline__ int g2p_slot(const Ws &ws, const int4 &ch) {
+    const int pos = ch.y + (int)threadIdx.x;
+    return ((int)threadIdx.x < ch.z && pos < ws.n) ? ws.order[pos] : 0;
+}
+
 template <int CH>
 __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ scenes, PState st,
                                                  PState out, Ws ws, float dt, int *status) {
-    __shared__ float4 tile[kTileNodes];
+    extern __shared__ __align__(16) unsigned char g2p_smem_raw[];
+    G2PSmem<CH> &sm = *reinterpret_cast<G2PSmem<CH> *>(g2p_smem_raw);
     const int n_chunks = *ws.n_chunks;
     const int sentinel = (ws.nbk - 1) * 64;  // out-of-domain cell key
-    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
-        const int4 ch = ws.chunks[c];
-        const int pos = ch.y + (int)threadIdx.x;  // sorted position of this thread's particle
+    int c = blockIdx.x;
+    if (c >= n_chunks) return;
+    int4 ch = ws.chunks[c];
+    int slot = g2p_slot(ws, ch);
+    g2p_prefetch<CH>(scenes, st, ws, ch, slot, sm, 0);
+    cp_async_commit();
+    int cn = c + gridDim.x;
+    int4 chn = make_int4(0, 0, 0, -1);
+    int slotn = 0;
+    if (cn < n_chunks) {
+        chn = ws.chunks[cn];
+        slotn = g2p_slot(ws, chn);
+    }
+    int buf = 0;
+    while (c < n_chunks) {
+        if (cn < n_chunks) g2p_prefetch<CH>(scenes, st, ws, chn, slotn, sm, buf ^ 1);
+        cp_async_commit();
+        // order[] indices two chunks ahead
+        const int cnn = cn + gridDim.x;
+        int4 chnn = make_int4(0, 0, 0, -1);
+        int slotnn = 0;
+        if (cnn < n_chunks) {
+            chnn = ws.chunks[cnn];
+            slotnn = g2p_slot(ws, chnn);
+        }
+        cp_async_wait1();
+        __syncthreads();
+
+        const int pos = ch.y + (int)threadIdx.x;
         const bool mine = (int)threadIdx.x < ch.z && pos < ws.n;
-        const int slot = mine ? ws.order[pos] : 0;
+        int key = -1;
         if (ch.w < 0) {  // out-of-domain particles: carry the records over (uniform per CTA)
             if (mine) {
 #pragma unroll
                 for (int q = 0; q < kRecQuads; ++q) strec(out, pos, q, ldrec(st, slot, q));
                 out.key[pos] = st.key[slot];
             }
-            continue;
-        }
-        const MpmScene &S = scenes[ch.w];
-        int bx, by, bz;
-        chunk_block(S, ch.x, bx, by, bz);
-        const int nb = S.n_blocks_axis;
-        // this thread's particle: issue its loads before the tile barrier
-        float x0[3], xo[3], Fp[9];
-        float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
-        if (mine) {
-            // record quads 0 (x0 m), 1 (vol uid yield F8), 2 (u), 8-9 (F0-7)
-            const float4 q2 = ldrec(st, slot, 2), q8 = ldrec(st, slot, 8), q9 = ldrec(st, slot, 9);
-            q0 = ldrec(st, slot, 0);
-            q1 = ldrec(st, slot, 1);
-            x0[0] = q0.x; x0[1] = q0.y; x0[2] = q0.z;
-            xo[0] = __fadd_rn(x0[0], q2.x);
-            xo[1] = __fadd_rn(x0[1], q2.y);
-            xo[2] = __fadd_rn(x0[2], q2.z);
-            Fp[0] = q8.x; Fp[1] = q8.y; Fp[2] = q8.z; Fp[3] = q8.w;
-            Fp[4] = q9.x; Fp[5] = q9.y; Fp[6] = q9.z; Fp[7] = q9.w; Fp[8] = q1.w;
-        }
-        for (int i = threadIdx.x; i < kTileNodes; i += CH) {
-            const int tx = i / 36, ty = (i / 6) % 6, tz = i % 6;
-            const int ix = 4 * bx + tx, iy = 4 * by + ty, iz = 4 * bz + tz;
-            float4 gv = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (ix < S.n_grid && iy < S.n_grid && iz < S.n_grid)
-                gv = ws.grid_v[node_addr(S.block_begin, nb, ix, iy, iz)];
-            tile[i] = gv;
-        }
-        __syncthreads();
-        int key = -1;
-        if (mine) {
+        } else if (mine) {
+            const MpmScene &S = scenes[ch.w];
+            int bx, by, bz;
+            chunk_block(S, ch.x, bx, by, bz);
+            const float4 *tile = sm.tile[buf];
+            const float4 q0 = sm.rec[buf][0][threadIdx.x], q1 = sm.rec[buf][1][threadIdx.x],
+                         q2 = sm.rec[buf][2][threadIdx.x], q8 = sm.rec[buf][3][threadIdx.x],
+                         q9 = sm.rec[buf][4][threadIdx.x];
+            const float x0[3] = {q0.x, q0.y, q0.z};
+            const float xo[3] = {__fadd_rn(q0.x, q2.x), __fadd_rn(q0.y, q2.y), __fadd_rn(q0.z, q2.z)};
+            const float Fp[9] = {q8.x, q8.y, q8.z, q8.w, q9.x, q9.y, q9.z, q9.w, q1.w};
             float gp[3];
             int base[3];
             bool ok = true;
@@ -346,11 +409,12 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
             }
             const int lx = base[0] - 4 * bx, ly = base[1] - 4 * by, lz = base[2] - 4 * bz;
             ok &= (unsigned)lx < 4u && (unsigned)ly < 4u && (unsigned)lz < 4u;
+            float4 *orec = sm.outrec + threadIdx.x * kOutStride;
             if (!ok) {
                 atomicOr(status, MPM_ST_INTERNAL);
                 key = sentinel;
 #pragma unroll
-                for (int q = 0; q < kRecQuads; ++q) strec(out, pos, q, ldrec(st, slot, q));
+                for (int q = 0; q < kRecQuads; ++q) orec[q] = ldrec(st, slot, q);
                 out.key[pos] = key;
             } else {
                 Weights W;
@@ -435,16 +499,16 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
 #pragma unroll
                 for (int k = 0; k < 9; ++k) chk += fabsf(Fo[k]) + fabsf(tau[k]);
                 if (!(S.material == MPM_METAL && S.hardening == 1)) yld = q1.z;
-                strec(out, pos, 0, q0);
-                strec(out, pos, 1, make_float4(q1.x, q1.y, yld, Fo[8]));
-                strec(out, pos, 2, make_float4(un[0], un[1], un[2], nv[0]));
-                strec(out, pos, 3, make_float4(nv[1], nv[2], nC[0], nC[1]));
-                strec(out, pos, 4, make_float4(nC[2], nC[3], nC[4], nC[5]));
-                strec(out, pos, 5, make_float4(nC[6], nC[7], nC[8], tau[0]));
-                strec(out, pos, 6, make_float4(tau[1], tau[2], tau[3], tau[4]));
-                strec(out, pos, 7, make_float4(tau[5], tau[6], tau[7], tau[8]));
-                strec(out, pos, 8, make_float4(Fo[0], Fo[1], Fo[2], Fo[3]));
-                strec(out, pos, 9, make_float4(Fo[4], Fo[5], Fo[6], Fo[7]));
+                orec[0] = q0;
+                orec[1] = make_float4(q1.x, q1.y, yld, Fo[8]);
+                orec[2] = make_float4(un[0], un[1], un[2], nv[0]);
+                orec[3] = make_float4(nv[1], nv[2], nC[0], nC[1]);
+                orec[4] = make_float4(nC[2], nC[3], nC[4], nC[5]);
+                orec[5] = make_float4(nC[6], nC[7], nC[8], tau[0]);
+                orec[6] = make_float4(tau[1], tau[2], tau[3], tau[4]);
+                orec[7] = make_float4(tau[5], tau[6], tau[7], tau[8]);
+                orec[8] = make_float4(Fo[0], Fo[1], Fo[2], Fo[3]);
+                orec[9] = make_float4(Fo[4], Fo[5], Fo[6], Fo[7]);
                 int flags = 0;
                 const float vmax = S.dx / dt;
                 if (fabsf(nv[0]) > vmax || fabsf(nv[1]) > vmax || fabsf(nv[2]) > vmax) flags |= MPM_ST_CFL;
@@ -458,12 +522,34 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
         }
         warp_histogram(ws.counts, ws.cell_counts, key);
         __syncthreads();
+        if (ch.w >= 0) {  // the chunk's records are contiguous in `out`: coalesced write-out
+            const int nq = min(ch.z, ws.n - ch.y) * kRecQuads;
+            float4 *dst = out.rec + (int64_t)ch.y * kRecQuads;
+            for (int l = threadIdx.x; l < nq; l += CH)
+                dst[l] = sm.outrec[(l / kRecQuads) * kOutStride + (l % kRecQuads)];
+        }
+        __syncthreads();  // buffer `buf` and outrec are refilled by the next iteration
+        c = cn; ch = chn; slot = slotn;
+        cn = cnn; chn = chnn; slotn = slotnn;
+        buf ^= 1;
     }
+    cp_async_wait0();
 }
 
 template <int CH>
 static cudaError_t g2p_t(const Ctx &cx, float dt, int grid) {
-    g2p_kernel<CH><<<grid, CH, 0, cx.stream>>>(cx.scenes, cx.st, cx.st2, cx.ws, dt, cx.status);
+    // more than the 48 KB of static shared memory: opt in once per instance and device
+    static bool attr_set[64] = {false};
+    const int bytes = (int)sizeof(G2PSmem<CH>);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
+        e = cudaFuncSetAttribute(g2p_kernel<CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        if (dev >= 0 && dev < 64) attr_set[dev] = true;
+    }
+    g2p_kernel<CH><<<grid, CH, bytes, cx.stream>>>(cx.scenes, cx.st, cx.st2, cx.ws, dt, cx.status);
     return cudaGetLastError();
 }
 
