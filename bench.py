@@ -241,6 +241,7 @@ def gb300_arm(args, sc, world, rank, local):
 
     gsize = 32
     graph = eng.graph(gsize, float(sim.time), dt)
+    graph.replay()  # untimed: the first replay uploads the graph
     torch.cuda.synchronize()
     st = torch.cuda.current_stream()
     K = args.steps
@@ -346,6 +347,8 @@ def gb300_arm(args, sc, world, rank, local):
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": None if traffic is None else traffic.get("bytes_per_substep"),
+                     "traffic_source": None if traffic is None else
+                     "profiles/dram_traffic_%s.json (ncu dram__bytes_read+write, one substep)" % sc.name,
                      "algorithmic_bytes_per_unit": alg, "unit_count": n, "peak_source": peak_src},
         "roofline_kernels": kern,
         "e2e": {"value": e2e_value, "unit": "particle-substeps/s", "h2d_bytes_per_step": 60 * n,
