@@ -366,11 +366,55 @@ def gb300_arm(args, sc, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def batched_arm(args):
+    """64 scenes (sand and metal, N log-uniform in [1e4, 2e5], grids 48/64/96) in one
+    batched launch per stage, against the same scenes stepped one by one."""
+    import torch
+
+    import __graft_entry__ as g
+    from reduced_mpm_stress_training_gb300 import scenarios as S
+    from reduced_mpm_stress_training_gb300.batched import BatchedMPM, time_chunk_size
+
+    g.build()
+    scenes = S.batch_64()
+    device = torch.device("cuda:0")
+    b = BatchedMPM(scenes, device=device, chunk_size="auto")
+    dt = scenes[0].dt
+    for _ in range(max(3, args.warmup)):
+        b.step(dt)
+    gsize = 32
+    graph = b.graph(gsize, dt)
+    graph.replay()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    K = max(gsize, args.steps - args.steps % gsize)
+    e0.record(st)
+    for _ in range(K // gsize):
+        graph.replay()
+    e1.record(st)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / K
+    seq = sum(time_chunk_size([s], b.chunk_size, device, steps=16) for s in scenes)
+    n = b.n_particles
+    print(json.dumps({"metric": "particle-substeps/s (64-scene batch, fp32)", "value": n / t,
+                      "unit": "particle-substeps/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * t, "higher_is_better": True, "dtype": "f32",
+                      "data": "synthetic", "config": {"workload": "batch_64", "scenes": len(scenes),
+                                                      "particles": n, "chunk_size": b.chunk_size},
+                      "one_by_one": {"value": n / seq, "ms_per_step": 1e3 * seq},
+                      "speedup_vs_one_by_one": seq / t, "status": b.engine.status()}), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
     from reduced_mpm_stress_training_gb300 import scenarios as S
 
+    if args.workload == "batch_64":
+        if rank == 0 and args.impl == "gb300":
+            batched_arm(args)
+        return
     sc = S.SCENES[args.workload]()
     if world > 1:
         import torch
