@@ -222,6 +222,37 @@ int mpm_svd3(const float *A, float *U, float *s, float *V, int64_t n, void *stre
 int mpm_return_map(const MpmScene *scene, const float *F_trial, float *yield, float *F,
                    float *stress, int64_t n, void *stream);
 
+/* ---- stress-surrogate network (12 -> 128 -> 128 -> 128 -> 6, SiLU) ---
+ * No counterpart in the reference's solver; the nearest relative is the
+ * stress decoder CROMnet_secondary.NetDec (CROMnet_secondary.py:203-301),
+ * whose 6-component output is stored as [xx, xy, xz, yy, yz, zz]
+ * (engine_stress/mpm_solver_warp.py:383).  BF16 weights and activations,
+ * FP32 accumulation on the tensor cores.  The parameter blob (device,
+ * mpm_mlp_param_bytes() bytes) holds bf16 weights W1 [128][16] (inputs
+ * 12..15 zero), W2, W3 [128][128], W4 [16][128] (outputs 6..15 zero),
+ * then fp32 biases b1, b2, b3 [128], b4 [16].  Gradients and the Adam
+ * master copy use the same order in fp32: MPM_MLP_PARAMS floats. */
+#define MPM_MLP_IN 12
+#define MPM_MLP_OUT 6
+#define MPM_MLP_HIDDEN 128
+#define MPM_MLP_PARAMS 37264 /* 36864 weights + 400 biases */
+int64_t mpm_mlp_param_bytes(void);
+
+/* y (n,6) = net(x (n,12)).  With target (n,6) != NULL also writes the
+ * loss gradient dy (n,16 bf16) = grad_scale * (y - target), the
+ * pre-activations zsave (3,n,128 bf16) for the backward pass, and adds
+ * the summed squared error to *loss (device float).  y may be NULL. */
+int mpm_mlp_forward(const void *params, const float *x, float *y, const float *target, void *zsave,
+                    void *dy, float *loss, float grad_scale, int64_t n, void *stream);
+/* Adds the parameter gradient of the forward's loss into grad (fp32,
+ * MPM_MLP_PARAMS).  work: 2*n*128 bf16 scratch. */
+int mpm_mlp_backward(const void *params, const float *x, const void *zsave, const void *dy, void *work,
+                     float *grad, int64_t n, void *stream);
+/* One Adam step (torch.optim.Adam semantics, step >= 1) on the fp32
+ * master parameters; rewrites the bf16/fp32 blob params from them. */
+int mpm_mlp_adam(float *master, float *m, float *v, const float *grad, void *params, float lr,
+                 float beta1, float beta2, float eps, int32_t step, void *stream);
+
 /* ---- misc ------------------------------------------------------------ */
 int mpm_abi_version(void);
 /* sizeof of the ABI structs, for binding checks: out[0..3] =

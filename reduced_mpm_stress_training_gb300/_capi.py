@@ -16,6 +16,7 @@ MPM_OK, MPM_ERR_ARG, MPM_ERR_CUDA, MPM_ERR_SIZE = 0, -1, -2, -3
 ST_OUT_OF_DOMAIN, ST_CFL, ST_NONFINITE, ST_INTERNAL = 1, 2, 4, 8
 JELLY, METAL, SAND = 0, 1, 2
 COLLIDER_SURFACE, COLLIDER_BOX = 0, 1
+MLP_IN, MLP_OUT, MLP_HIDDEN, MLP_PARAMS = 12, 6, 128, 37264
 
 (FIELD_X_INITIAL, FIELD_U, FIELD_V, FIELD_C, FIELD_F, FIELD_STRESS, FIELD_MASS, FIELD_VOL,
  FIELD_YIELD, FIELD_X, FIELD_F_DISP) = range(11)
@@ -80,6 +81,13 @@ _SIGS = {
     "mpm_svd3": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
     "mpm_return_map": ([C.POINTER(MpmScene), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                         C.c_int64, C.c_void_p], C.c_int),
+    "mpm_mlp_param_bytes": ([], C.c_int64),
+    "mpm_mlp_forward": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                         C.c_void_p, C.c_float, C.c_int64, C.c_void_p], C.c_int),
+    "mpm_mlp_backward": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                          C.c_int64, C.c_void_p], C.c_int),
+    "mpm_mlp_adam": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
+                      C.c_float, C.c_float, C.c_float, C.c_int32, C.c_void_p], C.c_int),
     "mpm_abi_version": ([], C.c_int),
     "mpm_struct_sizes": ([C.POINTER(C.c_int64)], None),
     "mpm_error_string": ([C.c_int], C.c_char_p),

@@ -79,13 +79,16 @@ def compare(sim, ref, fields=("x", "v", "C", "F", "stress")) -> dict:
 
 def within_fp32_floor(gpu, o32, o64, rtol=1e-5, k=3.0):
     """True when the GPU result is as close to the float32 oracle as the float32
-    oracle is to the float64 rerun (times k), or within rtol relative.  Used for
-    stress and C: near F = I they are dominated by float32 rounding of the SVD
-    (singular values carry ~1e-7 noise), the same in the reference."""
+    oracle is to the float64 rerun (times k), or within rtol relative; or when
+    the GPU result is itself within k times the float32 oracle's own error of
+    the float64 rerun (it is then as accurate as a float32 run can be).  Used
+    for stress, C and v: near F = I they are dominated by float32 rounding of
+    the SVD (singular values carry ~1e-7 noise), the same in the reference."""
     g, a, b = (np.asarray(x, np.float64).ravel() for x in (gpu, o32, o64))
     floor = np.linalg.norm(a - b)
     d32 = np.linalg.norm(g - a)
     d64 = np.linalg.norm(g - b)
     scale = max(np.linalg.norm(b), 1e-30)
-    ok = (d32 <= max(rtol * scale, k * floor)) and (d64 <= max(rtol * scale, k * floor) + floor)
+    lim = max(rtol * scale, k * floor)
+    ok = (d64 <= lim) or ((d32 <= lim) and (d64 <= lim + floor))
     return bool(ok), dict(gpu_vs_o32=d32 / scale, gpu_vs_o64=d64 / scale, o32_vs_o64=floor / scale)

@@ -1,0 +1,83 @@
+"""Network kernels (csrc/mpm_mlp.cu) against the NumPy oracle (oracle/mlp.py):
+forward outputs, loss, parameter gradients and the Adam update, on ragged
+batch sizes; then a short training run that must lower the loss."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import mlp as M
+from reduced_mpm_stress_training_gb300.surrogate import StressMLP
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def _data(n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((n, M.IN)).astype(np.float32)
+    t = (np.tanh(x[:, :M.OUT] * 0.7 + x[:, M.OUT:M.OUT * 2] * 0.3)).astype(np.float32)
+    return x, t
+
+
+@pytest.mark.parametrize("n", [1, 17, 1000, 4099])
+def test_forward_matches_oracle(cuda, n):
+    x, _ = _data(n, n)
+    net = StressMLP(cuda, seed=5)
+    y = net.forward(torch.from_numpy(x).to(cuda)).cpu().numpy()
+    ref = M.forward(net.master.cpu().numpy(), x)["y"]
+    # same bf16 rounding points; differences come from fp32 summation order
+    assert rel(y, ref) < 2e-3, rel(y, ref)
+
+
+@pytest.mark.parametrize("n", [33, 2048, 5000])
+def test_loss_and_gradient_match_oracle(cuda, n):
+    x, t = _data(n, 100 + n)
+    net = StressMLP(cuda, seed=7)
+    loss = net.loss_and_grad(torch.from_numpy(x).to(cuda), torch.from_numpy(t).to(cuda)).item()
+    p = net.master.cpu().numpy()
+    o = M.forward(p, x, t, 2.0 / (n * M.OUT))
+    g_ref = M.backward(p, o["cache"])
+    assert abs(loss - o["loss_sum"] / (n * M.OUT)) <= 1e-3 * abs(loss) + 1e-7
+    g = net.grad.cpu().numpy()
+    gw, gb = M.unpack(g)
+    rw, rb = M.unpack(g_ref)
+    for l in range(4):
+        assert rel(gw[l], rw[l]) < 1e-2, ("W", l, rel(gw[l], rw[l]))
+        assert rel(gb[l], rb[l]) < 1e-2, ("b", l, rel(gb[l], rb[l]))
+    # padded entries get no gradient
+    assert np.all(gw[0][:, M.IN:] == 0) and np.all(gw[3][M.OUT:, :] == 0) and np.all(gb[3][M.OUT:] == 0)
+
+
+def test_adam_step_matches_oracle(cuda):
+    x, t = _data(3000, 9)
+    net = StressMLP(cuda, seed=11)
+    p = net.master.cpu().numpy().copy()
+    m = np.zeros_like(p)
+    v = np.zeros_like(p)
+    for step in (1, 2, 3):
+        net.loss_and_grad(torch.from_numpy(x).to(cuda), torch.from_numpy(t).to(cuda))
+        g = net.grad.cpu().numpy()
+        net.adam(lr=1e-3)
+        M.adam(p, m, v, g, step)
+        assert np.allclose(net.master.cpu().numpy(), p, rtol=1e-5, atol=1e-7)
+    # the bf16 blob follows the master copy
+    blob = net.params.cpu()
+    w = blob[:M.W_COUNT * 2].view(torch.bfloat16).float().numpy()
+    assert np.array_equal(w, M.bf16(p[:M.W_COUNT]))
+
+
+def test_training_lowers_the_loss(cuda):
+    x, t = _data(65536, 3)
+    xt = torch.from_numpy(x).to(cuda)
+    tt = torch.from_numpy(t).to(cuda)
+    net = StressMLP(cuda, seed=0)
+    first = net.train_step(xt, tt).item()
+    for _ in range(300):
+        last = net.train_step(xt, tt)
+    last = last.item()
+    assert last < 0.1 * first, (first, last)
