@@ -253,6 +253,65 @@ int mpm_mlp_backward(const void *params, const float *x, const void *zsave, cons
 int mpm_mlp_adam(float *master, float *m, float *v, const float *grad, void *params, float lr,
                  float beta1, float beta2, float eps, int32_t step, void *stream);
 
+/* ---- surrogate stress step ------------------------------------------
+ * A substep whose Drucker-Prager return map + Kirchhoff stress
+ * (engine_stress/mpm_utils.py:45-52, :87-112, called from
+ * g2p_apic_and_stress :284-306) comes from the network instead of the SVD.
+ * Network input (12): the 9 entries of Bhat = (F F^T - I) / rho with
+ * rho = ||F F^T - I||_F, then (log10 rho + 2.5) / 1.5, (nu - 0.3) / 0.1 and
+ * (friction angle in degrees - 30) / 10, nu and the angle recovered from
+ * the scene's lam, mu and alpha.  Output (6): tau / (mu rho) as
+ * [xx, xy, xz, yy, yz, zz].  The network's stress is corrected to the exact
+ * mean stress and deviatoric norm (closed-form eigenvalues of F F^T, no
+ * SVD); a particle falls back to the SVD return map when it leaves the
+ * training domain, reaches the cone apex, takes a plastic increment above
+ * dgamma_max, or when its error estimate (max of the correction size, the
+ * non-coaxiality of the deviator with F F^T and its Lode-angle mismatch)
+ * exceeds tol.  Non-sand scenes always take the SVD path. */
+typedef struct MpmSurrogateConfig {
+    float tol;                /* gate on the relative error estimate (1e-2)          */
+    float rho_min, rho_max;   /* domain of ||F F^T - I||_F                           */
+    float nu_min, nu_max;     /* domain of Poisson's ratio                           */
+    float phi_min, phi_max;   /* domain of the friction angle, degrees               */
+    float dgamma_max;         /* larger plastic increments fall back                 */
+} MpmSurrogateConfig;
+
+/* stats[] slots (int32, device): per-particle outcome counts, accumulated
+ * across calls (the caller zeroes them), and the fallback count of the
+ * last call (reset by each call). */
+#define MPM_SUR_ELASTIC 0    /* accepted, elastic (F = F_trial)                  */
+#define MPM_SUR_PLASTIC 1    /* accepted, on the cone (F = exp(-dgamma N) F_trial) */
+#define MPM_SUR_FB_DOMAIN 2  /* fallback: outside the training domain           */
+#define MPM_SUR_FB_APEX 3    /* fallback: projection to the cone apex            */
+#define MPM_SUR_FB_STEP 4    /* fallback: plastic increment above dgamma_max     */
+#define MPM_SUR_FB_GATE 5    /* fallback: error estimate above tol               */
+#define MPM_SUR_FB_MATERIAL 6 /* fallback: material other than sand             */
+#define MPM_SUR_LAST_FALLBACKS 7
+#define MPM_SUR_STATS 8
+
+/* Training tuples from F_trial (n,9), the scene's material and the plain
+ * return map's stress (n,9) (mpm_return_map): x (n,12) network inputs,
+ * y (n,6) targets tau / (mu rho).  stress may be NULL (then y is not
+ * written). */
+int mpm_surrogate_features(const MpmScene *scene, const float *F, const float *stress, float *x,
+                           float *y, int64_t n, void *stream);
+
+/* The surrogate on plain arrays of one scene: F_trial (n,9) -> F (n,9),
+ * stress (n,9) and the outcome code (n, MPM_SUR_*) of each row; rows the
+ * gate rejects are computed by the SVD return map (as mpm_return_map). */
+int mpm_surrogate_apply(const MpmScene *scene, const void *mlp_params, const MpmSurrogateConfig *cfg,
+                        const float *F_trial, float *F, float *stress, int32_t *codes, int64_t n,
+                        void *stream);
+
+/* G2P with the surrogate stress stage (replaces mpm_g2p in a substep).
+ * fallback: device scratch of 2 * n_particles int32.  stats: MPM_SUR_STATS
+ * device int32.  mlp_params: the network blob (mpm_mlp_param_bytes). */
+int mpm_g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogateConfig *cfg,
+                      void *fallback, int32_t *stats, float dt, void *stream);
+/* mpm_p2g2p with mpm_g2p_surrogate in place of mpm_g2p. */
+int mpm_p2g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogateConfig *cfg,
+                        void *fallback, int32_t *stats, float time, float dt, void *stream);
+
 /* ---- misc ------------------------------------------------------------ */
 int mpm_abi_version(void);
 /* sizeof of the ABI structs, for binding checks: out[0..3] =

@@ -44,11 +44,13 @@ def bf16(a: np.ndarray) -> np.ndarray:
 
 
 def silu(z):
-    return z / (1.0 + np.exp(-z))
+    """z sigmoid(z), sigmoid written as (1 + tanh(z/2)) / 2 as the kernels do
+    (they evaluate tanh with the hardware approximation)."""
+    return z * (0.5 + 0.5 * np.tanh(0.5 * z))
 
 
 def silu_grad(z):
-    s = 1.0 / (1.0 + np.exp(-z))
+    s = 0.5 + 0.5 * np.tanh(0.5 * z)
     return s * (1.0 + z * (1.0 - s))
 
 

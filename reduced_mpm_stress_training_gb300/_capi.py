@@ -59,6 +59,17 @@ class MpmBuffers(C.Structure):
                 ("substep", C.c_int64)]
 
 
+class MpmSurrogateConfig(C.Structure):
+    _fields_ = [("tol", C.c_float), ("rho_min", C.c_float), ("rho_max", C.c_float),
+                ("nu_min", C.c_float), ("nu_max", C.c_float), ("phi_min", C.c_float),
+                ("phi_max", C.c_float), ("dgamma_max", C.c_float)]
+
+
+(SUR_ELASTIC, SUR_PLASTIC, SUR_FB_DOMAIN, SUR_FB_APEX, SUR_FB_STEP, SUR_FB_GATE,
+ SUR_FB_MATERIAL, SUR_LAST_FALLBACKS) = range(8)
+SUR_STATS = 8
+
+
 class MPMLibraryError(RuntimeError):
     """A libmpm_gb300 call returned an error code."""
 
@@ -88,6 +99,14 @@ _SIGS = {
                           C.c_int64, C.c_void_p], C.c_int),
     "mpm_mlp_adam": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
                       C.c_float, C.c_float, C.c_float, C.c_int32, C.c_void_p], C.c_int),
+    "mpm_surrogate_features": ([C.POINTER(MpmScene), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_int64, C.c_void_p], C.c_int),
+    "mpm_surrogate_apply": ([C.POINTER(MpmScene), C.c_void_p, C.POINTER(MpmSurrogateConfig), C.c_void_p,
+                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
+    "mpm_g2p_surrogate": ([C.POINTER(MpmBuffers), C.c_void_p, C.POINTER(MpmSurrogateConfig),
+                           C.c_void_p, C.c_void_p, C.c_float, C.c_void_p], C.c_int),
+    "mpm_p2g2p_surrogate": ([C.POINTER(MpmBuffers), C.c_void_p, C.POINTER(MpmSurrogateConfig),
+                             C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "mpm_abi_version": ([], C.c_int),
     "mpm_struct_sizes": ([C.POINTER(C.c_int64)], None),
     "mpm_error_string": ([C.c_int], C.c_char_p),

@@ -288,6 +288,57 @@ int mpm_p2g2p(MpmBuffers *b, float time, float dt, void *stream) {
     return mpm_g2p(b, dt, stream);
 }
 
+static bool surrogate_cfg_ok(const MpmSurrogateConfig *c) {
+    // dgamma_max <= 0.25 keeps the exp series of the plastic F update exact to 1e-8
+    return c && c->tol >= 0.0f && c->rho_min >= 0.0f && c->rho_min <= c->rho_max &&
+           c->nu_min <= c->nu_max && c->phi_min <= c->phi_max && c->dgamma_max >= 0.0f &&
+           c->dgamma_max <= 0.25f;
+}
+
+int mpm_surrogate_features(const MpmScene *scene, const float *F, const float *stress, float *x, float *y,
+                           int64_t n, void *stream) {
+    if (!scene || n < 0 || (n > 0 && (!F || !x || (stress && !y)))) return MPM_ERR_ARG;
+    if (!(scene->mu > 0.0f)) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_features(*scene, F, stress, x, y, n, static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
+int mpm_surrogate_apply(const MpmScene *scene, const void *mlp_params, const MpmSurrogateConfig *cfg,
+                        const float *F_trial, float *F, float *stress, int32_t *codes, int64_t n, void *stream) {
+    if (!scene || !mlp_params || !surrogate_cfg_ok(cfg) || n < 0) return MPM_ERR_ARG;
+    if (n > 0 && (!F_trial || !F || !stress || !codes)) return MPM_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(mlp_params) & 15) return MPM_ERR_ARG;
+    int dev = 0, sms = 0;
+    MPM_CHECK(cudaGetDevice(&dev));
+    MPM_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    MPM_CHECK(mpm::launch_surrogate_apply(*scene, mlp_params, *cfg, F_trial, F, stress, codes, n, sms,
+                                          static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
+int mpm_g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogateConfig *cfg, void *fallback,
+                      int32_t *stats, float dt, void *stream) {
+    if (!buffers_ok(b) || !mlp_params || !surrogate_cfg_ok(cfg) || !stats) return MPM_ERR_ARG;
+    if (b->plan.n_particles > 0 && (!fallback || (reinterpret_cast<uintptr_t>(fallback) & 7))) return MPM_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(mlp_params) & 15) return MPM_ERR_ARG;
+    mpm::Ctx cx = make_ctx(b, stream, b->cur);
+    MPM_CHECK(mpm::launch_g2p(cx, dt, true));
+    MPM_CHECK(mpm::launch_surrogate(cx, mlp_params, *cfg, static_cast<int2 *>(fallback), stats));
+    b->cur ^= 1;  // as mpm_g2p: the updated records are in the other buffer
+    b->substep += 1;
+    return MPM_OK;
+}
+
+int mpm_p2g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogateConfig *cfg, void *fallback,
+                        int32_t *stats, float time, float dt, void *stream) {
+    if (!buffers_ok(b) || !mlp_params || !surrogate_cfg_ok(cfg) || !stats) return MPM_ERR_ARG;
+    int r = mpm_sort(b, stream);
+    if (r) return r;
+    if ((r = mpm_p2g(b, dt, stream))) return r;
+    if ((r = mpm_grid_update(b, time, dt, stream))) return r;
+    return mpm_g2p_surrogate(b, mlp_params, cfg, fallback, stats, dt, stream);
+}
+
 int mpm_export_grid(MpmBuffers *b, int32_t scene, float *grid_m, float *grid_v_in,
                     float *grid_v_out, void *stream) {
     if (!buffers_ok(b) || scene < 0 || scene >= b->plan.n_scenes) return MPM_ERR_ARG;

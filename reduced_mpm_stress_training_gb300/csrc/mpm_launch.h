@@ -28,7 +28,19 @@ cudaError_t launch_sort(const Ctx &cx);
 // transfer stages (mpm_substep.cu)
 cudaError_t launch_p2g(const Ctx &cx, float dt);
 cudaError_t launch_grid(const Ctx &cx, float time, float dt);
-cudaError_t launch_g2p(const Ctx &cx, float dt);
+// defer_stress: store F_trial as F and skip the return map (surrogate stage follows)
+cudaError_t launch_g2p(const Ctx &cx, float dt, bool defer_stress = false);
+
+// surrogate stress stage (mpm_surrogate.cu): network stress with exact-invariant
+// correction and gating on the records G2P wrote into cx.st2; fallbacks to the
+// SVD return map.  stats: 8 device ints (see mpm_g2p_surrogate).
+cudaError_t launch_surrogate(const Ctx &cx, const void *mlp_params, const MpmSurrogateConfig &cfg,
+                             int2 *fallback, int *stats);
+cudaError_t launch_surrogate_apply(const MpmScene &scene, const void *mlp_params, const MpmSurrogateConfig &cfg,
+                                   const float *F, float *Fo, float *tau, int *codes, int64_t n, int num_sms,
+                                   cudaStream_t stream);
+cudaError_t launch_features(const MpmScene &scene, const float *F, const float *stress, float *x, float *y,
+                            int64_t n, cudaStream_t stream);
 
 // data movement and element kernels (mpm_io.cu)
 cudaError_t launch_init_state(const Ctx &cx, const PState &other);

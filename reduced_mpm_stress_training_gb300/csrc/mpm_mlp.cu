@@ -14,144 +14,16 @@
 //   mlp_dgrad_kernel    dZ_l = (dZ_{l+1} W_{l+1}) * silu'(Z_l)
 //   mlp_wgrad_kernel    dW_l += dZ_l^T H_{l-1}, db_l += sum dZ_l   (row-split, fp32 atomics)
 //   mlp_adam_kernel     Adam on fp32 master weights, refreshes the bf16 copy
-#include <cuda_bf16.h>
-#include <stdint.h>
-
+#include "mpm_mlp.cuh"
 #include "mpm_launch.h"
 
 namespace mpm {
 namespace mlp {
 
-constexpr int IN = 12, K1 = 16, H = 128, OUT = 6, N4 = 16;
-constexpr int W1_OFF = 0, W2_OFF = W1_OFF + H * K1, W3_OFF = W2_OFF + H * H, W4_OFF = W3_OFF + H * H,
-              W_COUNT = W4_OFF + N4 * H;  // bf16 elements
-constexpr int B1_OFF = 0, B2_OFF = H, B3_OFF = 2 * H, B4_OFF = 3 * H, B_COUNT = 3 * H + N4;  // f32
-constexpr int64_t PARAM_BYTES = (int64_t)W_COUNT * 2 + (int64_t)B_COUNT * 4;
-constexpr int LDW = H + 8;   // padded smem row (bf16) of a 128-wide matrix: conflict-free ldmatrix
-constexpr int LDW1 = K1 + 8; // padded smem row of W1
-
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + expf(-z)); }
-__device__ __forceinline__ float silu_grad(float z) {
-    const float s = 1.0f / (1.0f + expf(-z));
-    return s * (1.0f + z * (1.0f - s));
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // .x = lo (low half)
-    return *reinterpret_cast<uint32_t *>(&v);
-}
-__device__ __forceinline__ float2 unpack_bf16(uint32_t u) {
-    __nv_bfloat162 v = *reinterpret_cast<__nv_bfloat162 *>(&u);
-    return __bfloat1622float2(v);
-}
-
-__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-        "{%8,%9}, {%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void ldsm_x4(uint32_t r[4], const void *p) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_u32(p)));
-}
-__device__ __forceinline__ void ldsm_x4_trans(uint32_t r[4], const void *p) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_u32(p)));
-}
-__device__ __forceinline__ void ldsm_x2(uint32_t r[2], const void *p) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n"
-                 : "=r"(r[0]), "=r"(r[1])
-                 : "r"(smem_u32(p)));
-}
-__device__ __forceinline__ void ldsm_x2_trans(uint32_t r[2], const void *p) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
-                 : "=r"(r[0]), "=r"(r[1])
-                 : "r"(smem_u32(p)));
-}
-
-// ---------------------------------------------------------------------------
-// Weights in shared memory, rows padded for conflict-free ldmatrix.
-// ---------------------------------------------------------------------------
-struct WSmem {
-    __nv_bfloat16 w1[H * LDW1];
-    __nv_bfloat16 w2[H * LDW];
-    __nv_bfloat16 w3[H * LDW];
-    __nv_bfloat16 w4[N4 * LDW];
-    float b[B_COUNT];
-};
-
-__device__ void load_weights(WSmem &s, const __nv_bfloat16 *w, const float *b) {
-    for (int i = threadIdx.x; i < H * K1; i += blockDim.x) s.w1[(i / K1) * LDW1 + i % K1] = w[W1_OFF + i];
-    for (int i = threadIdx.x; i < H * H; i += blockDim.x) {
-        s.w2[(i / H) * LDW + i % H] = w[W2_OFF + i];
-        s.w3[(i / H) * LDW + i % H] = w[W3_OFF + i];
-    }
-    for (int i = threadIdx.x; i < N4 * H; i += blockDim.x) s.w4[(i / H) * LDW + i % H] = w[W4_OFF + i];
-    for (int i = threadIdx.x; i < B_COUNT; i += blockDim.x) s.b[i] = b[i];
-}
-
-// B fragment (n8 x k16, "col" operand) from a weight matrix stored [n][k]:
-// lanes 0-7 address rows n0..n0+7 at k0, lanes 8-15 at k0+8.
-__device__ __forceinline__ void b_frag(uint32_t r[2], const __nv_bfloat16 *w, int ld, int n0, int k0) {
-    const int l = threadIdx.x & 15;
-    ldsm_x2(r, w + (n0 + (l & 7)) * ld + k0 + ((l >> 3) << 3));
-}
-
-// One dense layer on a warp's 16 rows: acc[nt][4] = A(16 x K) * W^T, W [128][K] in smem.
-template <int KT>  // number of k16 steps
-__device__ __forceinline__ void layer_mma(float acc[16][4], const uint32_t a[KT][4], const __nv_bfloat16 *w,
-                                          int ld) {
-#pragma unroll
-    for (int nt = 0; nt < 16; ++nt) {
-        acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) {
-            uint32_t b[2];
-            b_frag(b, w, ld, nt * 8, kt * 16);
-            mma16816(acc[nt], a[kt], b[0], b[1]);
-        }
-    }
-}
-
-// bias + SiLU on accumulators, then pack as the A fragments (k = the 128 features)
-// of the next layer; optionally save the pre-activations Z (bf16, row-major [rows][128]).
-__device__ __forceinline__ void act_to_a(float acc[16][4], const float *bias, uint32_t a[8][4],
-                                         __nv_bfloat16 *zsave, int64_t row0, int64_t n_rows) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int nt = 0; nt < 16; ++nt) {
-        const int col = nt * 8 + 2 * t;
-        const float z0 = acc[nt][0] + bias[col], z1 = acc[nt][1] + bias[col + 1];
-        const float z2 = acc[nt][2] + bias[col], z3 = acc[nt][3] + bias[col + 1];
-        if (zsave) {
-            if (row0 + g < n_rows)
-                *reinterpret_cast<uint32_t *>(zsave + (row0 + g) * H + col) = pack_bf16(z0, z1);
-            if (row0 + g + 8 < n_rows)
-                *reinterpret_cast<uint32_t *>(zsave + (row0 + g + 8) * H + col) = pack_bf16(z2, z3);
-        }
-        acc[nt][0] = silu(z0); acc[nt][1] = silu(z1); acc[nt][2] = silu(z2); acc[nt][3] = silu(z3);
-    }
-#pragma unroll
-    for (int kt = 0; kt < 8; ++kt) {
-        a[kt][0] = pack_bf16(acc[2 * kt][0], acc[2 * kt][1]);
-        a[kt][1] = pack_bf16(acc[2 * kt][2], acc[2 * kt][3]);
-        a[kt][2] = pack_bf16(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
-        a[kt][3] = pack_bf16(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
-    }
-}
-
 // Forward of a warp's 16 rows whose 12 inputs are x(row, i); writes outputs y(row, j).
 // Optional: save Z1..Z3 (training) and the loss gradient dY = 2 (y - target) * scale.
 struct FwdIO {
-    const float *x;        // [n][12] or null (then x comes from a functor in the caller)
+    const float *x;        // [n][12]
     float *y;              // [n][6]
     const float *target;   // [n][6] or null
     __nv_bfloat16 *z;      // [3][n][128] or null
@@ -161,29 +33,11 @@ struct FwdIO {
     int64_t n;
 };
 
-__device__ __forceinline__ void mlp_rows(const WSmem &s, const float xin[2][2][2][2] /*unused*/,
-                                         uint32_t a1[1][4], int64_t row0, const FwdIO &io) {
+__device__ __forceinline__ void mlp_rows(const WSmem &s, const uint32_t a1[1][4], int64_t row0,
+                                         const FwdIO &io) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    float acc[16][4];
-    uint32_t a[8][4];
-    layer_mma<1>(acc, a1, s.w1, LDW1);
-    act_to_a(acc, s.b + B1_OFF, a, io.z ? io.z + 0 * io.n * H : nullptr, row0, io.n);
-    layer_mma<8>(acc, a, s.w2, LDW);
-    act_to_a(acc, s.b + B2_OFF, a, io.z ? io.z + 1 * io.n * H : nullptr, row0, io.n);
-    layer_mma<8>(acc, a, s.w3, LDW);
-    act_to_a(acc, s.b + B3_OFF, a, io.z ? io.z + 2 * io.n * H : nullptr, row0, io.n);
-    // output layer: N = 16 (two n8 tiles), K = 128
     float out[2][4];
-#pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {
-        out[nt][0] = out[nt][1] = out[nt][2] = out[nt][3] = 0.0f;
-#pragma unroll
-        for (int kt = 0; kt < 8; ++kt) {
-            uint32_t b[2];
-            b_frag(b, s.w4, LDW, nt * 8, kt * 16);
-            mma16816(out[nt], a[kt], b[0], b[1]);
-        }
-    }
+    mlp_core(s, a1, out, io.z, row0, io.n);
     float lsum = 0.0f;
 #pragma unroll
     for (int nt = 0; nt < 2; ++nt) {
@@ -193,7 +47,7 @@ __device__ __forceinline__ void mlp_rows(const WSmem &s, const float xin[2][2][2
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 const int col = nt * 8 + 2 * t + e;
-                const float yv = out[nt][2 * h + e] + s.b[B4_OFF + col];
+                const float yv = out[nt][2 * h + e];
                 float d = 0.0f;
                 if (col < OUT && row < io.n) {
                     if (io.y) io.y[row * OUT + col] = yv;
@@ -245,7 +99,7 @@ __global__ void __launch_bounds__(256) mlp_forward_kernel(const __nv_bfloat16 *_
     for (int64_t tile = (int64_t)blockIdx.x * nwarps + warp; tile < tiles; tile += (int64_t)gridDim.x * nwarps) {
         uint32_t a1[1][4];
         a1_from_x(a1, io.x, tile * 16, io.n);
-        mlp_rows(s, nullptr, a1, tile * 16, io);
+        mlp_rows(s, a1, tile * 16, io);
     }
 }
 
@@ -263,16 +117,20 @@ __global__ void __launch_bounds__(128) mlp_dgrad_kernel(const __nv_bfloat16 *__r
     extern __shared__ __align__(16) unsigned char mlp_smem[];
     __nv_bfloat16 *ws = reinterpret_cast<__nv_bfloat16 *>(mlp_smem);  // [NN][LDW]
     __nv_bfloat16 (*as)[16 * LDA] = reinterpret_cast<__nv_bfloat16 (*)[16 * LDA]>(ws + NN * LDW);
-    for (int i = threadIdx.x; i < NN * H; i += blockDim.x) ws[(i / H) * LDW + i % H] = wnext[i];
+    for (int i = threadIdx.x; i < NN * (H / 8); i += blockDim.x)
+        *reinterpret_cast<uint4 *>(ws + (i / (H / 8)) * LDW + (i % (H / 8)) * 8) =
+            reinterpret_cast<const uint4 *>(wnext)[i];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     __syncthreads();
     const int64_t tiles = (n + 15) / 16;
     for (int64_t tile = (int64_t)blockIdx.x * 4 + warp; tile < tiles; tile += (int64_t)gridDim.x * 4) {
         const int64_t row0 = tile * 16;
         __nv_bfloat16 *a_s = as[warp];
-        for (int i = lane; i < 16 * NN; i += 32) {
-            const int r = i / NN, c = i % NN;
-            a_s[r * LDA + c] = (row0 + r < n) ? dz_next[(row0 + r) * NN + c] : __float2bfloat16_rn(0.0f);
+        for (int i = lane; i < 16 * (NN / 8); i += 32) {
+            const int r = i / (NN / 8), c = i % (NN / 8);
+            const uint4 v = (row0 + r < n) ? reinterpret_cast<const uint4 *>(dz_next + (row0 + r) * NN)[c]
+                                           : make_uint4(0u, 0u, 0u, 0u);
+            *reinterpret_cast<uint4 *>(a_s + r * LDA + c * 8) = v;
         }
         __syncwarp();
         float acc[16][4];
@@ -338,18 +196,34 @@ __global__ void __launch_bounds__(128) mlp_wgrad_kernel(const __nv_bfloat16 *__r
     const int64_t r_end = min(n, r_begin + rows_per_cta);
     for (int64_t r0 = r_begin; r0 < r_end; r0 += RT) {
         __syncthreads();
-        for (int i = threadIdx.x; i < RT * NO; i += blockDim.x) {
-            const int r = i / NO, c = i % NO;
-            ds[r * LDD + c] = (r0 + r < r_end) ? dz[(r0 + r) * NO + c] : __float2bfloat16_rn(0.0f);
+        for (int i = threadIdx.x; i < RT * (NO / 8); i += blockDim.x) {
+            const int r = i / (NO / 8), c = i % (NO / 8);
+            const uint4 v = (r0 + r < r_end) ? reinterpret_cast<const uint4 *>(dz + (r0 + r) * NO)[c]
+                                             : make_uint4(0u, 0u, 0u, 0u);
+            *reinterpret_cast<uint4 *>(ds + r * LDD + c * 8) = v;
         }
-        for (int i = threadIdx.x; i < RT * KI; i += blockDim.x) {
-            const int r = i / KI, c = i % KI;
-            float v = 0.0f;
-            if (r0 + r < r_end) {
-                if (FIRST) v = c < IN ? x[(r0 + r) * IN + c] : 0.0f;
-                else v = silu(__bfloat162float(zp[(r0 + r) * KI + c]));
+        if (FIRST) {
+            for (int i = threadIdx.x; i < RT * KI; i += blockDim.x) {
+                const int r = i / KI, c = i % KI;
+                const float v = (r0 + r < r_end && c < IN) ? x[(r0 + r) * IN + c] : 0.0f;
+                hs[r * LDH + c] = __float2bfloat16_rn(v);
             }
-            hs[r * LDH + c] = __float2bfloat16_rn(v);
+        } else {
+            // H = bf16(silu(Z)), eight activations per 16-byte word
+            for (int i = threadIdx.x; i < RT * (KI / 8); i += blockDim.x) {
+                const int r = i / (KI / 8), c = i % (KI / 8);
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (r0 + r < r_end) {
+                    v = reinterpret_cast<const uint4 *>(zp + (r0 + r) * KI)[c];
+                    uint32_t *u = reinterpret_cast<uint32_t *>(&v);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const float2 zz = unpack_bf16(u[k]);
+                        u[k] = pack_bf16(silu(zz.x), silu(zz.y));
+                    }
+                }
+                *reinterpret_cast<uint4 *>(hs + r * LDH + c * 8) = v;
+            }
         }
         __syncthreads();
         if (threadIdx.x < NO)
@@ -426,9 +300,19 @@ __global__ void mlp_adam_kernel(float *__restrict__ master, float *__restrict__ 
 
 using namespace mpm::mlp;
 
-static int mlp_grid(int64_t tiles, int per_cta) {
-    int64_t want = (tiles + per_cta - 1) / per_cta;
-    return (int)(want < 1 ? 1 : (want > 152 * 4 ? 152 * 4 : want));
+static int num_sms() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+        return 1;
+    return n;
+}
+
+// persistent grids: at most `per_sm` CTAs per SM, never more CTAs than work
+static int mlp_grid(int64_t tiles, int tiles_per_cta, int per_sm) {
+    const int64_t want = (tiles + tiles_per_cta - 1) / tiles_per_cta;
+    const int64_t cap = (int64_t)num_sms() * per_sm;
+    return (int)(want < 1 ? 1 : (want > cap ? cap : want));
 }
 
 template <int NN>
@@ -465,13 +349,14 @@ int64_t mpm_mlp_param_bytes(void) { return PARAM_BYTES; }
 int mpm_mlp_forward(const void *params, const float *x, float *y, const float *target,
                     void *zsave, void *dy, float *loss, float grad_scale, int64_t n, void *stream) {
     if (!params || n < 0 || (n > 0 && !x)) return MPM_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(params) & 15) return MPM_ERR_ARG;
     if (n == 0) return MPM_OK;
     if (mlp_attrs() != cudaSuccess) return MPM_ERR_CUDA;
     const __nv_bfloat16 *w = static_cast<const __nv_bfloat16 *>(params);
     const float *b = reinterpret_cast<const float *>(static_cast<const char *>(params) + (int64_t)W_COUNT * 2);
     FwdIO io{x, y, target, static_cast<__nv_bfloat16 *>(zsave), static_cast<__nv_bfloat16 *>(dy), loss,
              grad_scale, n};
-    mlp_forward_kernel<<<mlp_grid((n + 15) / 16, 8), 256, sizeof(WSmem), static_cast<cudaStream_t>(stream)>>>(
+    mlp_forward_kernel<<<mlp_grid((n + 15) / 16, 8, 1), 256, sizeof(WSmem), static_cast<cudaStream_t>(stream)>>>(
         w, b, io);
     return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
@@ -481,6 +366,7 @@ int mpm_mlp_forward(const void *params, const float *x, float *y, const float *t
 int mpm_mlp_backward(const void *params, const float *x, const void *zsave, const void *dy, void *work,
                      float *grad, int64_t n, void *stream) {
     if (!params || !x || !zsave || !dy || !work || !grad || n <= 0) return MPM_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(params) & 15) return MPM_ERR_ARG;
     if (mlp_attrs() != cudaSuccess) return MPM_ERR_CUDA;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const __nv_bfloat16 *w = static_cast<const __nv_bfloat16 *>(params);
@@ -494,7 +380,7 @@ int mpm_mlp_backward(const void *params, const float *x, const void *zsave, cons
     if (rows64 < 64) rows64 = 64;
     const int rows = (int)rows64;
     const int gridw = (int)((n + rows - 1) / rows);
-    const int gridd = mlp_grid((n + 15) / 16, 4);
+    const int gridd = mlp_grid((n + 15) / 16, 4, 4);
     const __nv_bfloat16 *dyb = static_cast<const __nv_bfloat16 *>(dy);
     // layer 4: dW4 += dY^T H3, dZ3 = (dY W4) * silu'(Z3)
     mlp_wgrad_kernel<N4, H, false><<<gridw, 128, 0, st>>>(dyb, z + 2 * n * H, nullptr, gw + W4_OFF, gb + B4_OFF, n, rows);

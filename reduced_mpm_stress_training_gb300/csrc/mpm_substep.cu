@@ -344,7 +344,9 @@ __device__ __forceinline__ int g2p_slot(const Ws &ws, const int4 &ch) {
     return ((int)threadIdx.x < ch.z && pos < ws.n) ? ws.order[pos] : 0;
 }
 
-template <int CH>
+// DEFER: leave the return map and stress to a later pass (the surrogate stress
+// stage): F_trial is stored as F and the stress words are zeroed.
+template <int CH, bool DEFER>
 __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ scenes, PState st,
                                                  PState out, Ws ws, float dt, int *status) {
     extern __shared__ __align__(16) unsigned char g2p_smem_raw[];
@@ -493,7 +495,15 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
                                         A[r * 3 + 2] * Fp[2 * 3 + q];
                 float yld = (S.material == MPM_METAL) ? q1.z : 0.0f;
                 float Fo[9], tau[9];
-                return_map_stress(S, Ft, yld, Fo, tau);
+                if (DEFER) {
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) {
+                        Fo[k] = Ft[k];
+                        tau[k] = 0.0f;
+                    }
+                } else {
+                    return_map_stress(S, Ft, yld, Fo, tau);
+                }
                 // stores: record quads 1-9
                 float chk = 0.0f;
 #pragma unroll
@@ -536,7 +546,7 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
     cp_async_wait0();
 }
 
-template <int CH>
+template <int CH, bool DEFER>
 static cudaError_t g2p_t(const Ctx &cx, float dt, int grid) {
     // more than the 48 KB of static shared memory: opt in once per instance and device
     static bool attr_set[64] = {false};
@@ -545,11 +555,11 @@ static cudaError_t g2p_t(const Ctx &cx, float dt, int grid) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64 || !attr_set[dev]) {
-        e = cudaFuncSetAttribute(g2p_kernel<CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        e = cudaFuncSetAttribute(g2p_kernel<CH, DEFER>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
         if (dev >= 0 && dev < 64) attr_set[dev] = true;
     }
-    g2p_kernel<CH><<<grid, CH, bytes, cx.stream>>>(cx.scenes, cx.st, cx.st2, cx.ws, dt, cx.status);
+    g2p_kernel<CH, DEFER><<<grid, CH, bytes, cx.stream>>>(cx.scenes, cx.st, cx.st2, cx.ws, dt, cx.status);
     return cudaGetLastError();
 }
 
@@ -575,15 +585,20 @@ cudaError_t launch_grid(const Ctx &cx, float time, float dt) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_g2p(const Ctx &cx, float dt) {
+template <bool DEFER>
+static cudaError_t g2p_sized(const Ctx &cx, float dt) {
     const int grid = persistent_grid(cx, 1024 / cx.ws.chunk_size);
     switch (cx.ws.chunk_size) {
-        case 32: return g2p_t<32>(cx, dt, grid);
-        case 64: return g2p_t<64>(cx, dt, grid);
-        case 128: return g2p_t<128>(cx, dt, grid);
-        case 256: return g2p_t<256>(cx, dt, grid);
+        case 32: return g2p_t<32, DEFER>(cx, dt, grid);
+        case 64: return g2p_t<64, DEFER>(cx, dt, grid);
+        case 128: return g2p_t<128, DEFER>(cx, dt, grid);
+        case 256: return g2p_t<256, DEFER>(cx, dt, grid);
         default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_g2p(const Ctx &cx, float dt, bool defer_stress) {
+    return defer_stress ? g2p_sized<true>(cx, dt) : g2p_sized<false>(cx, dt);
 }
 
 }  // namespace mpm

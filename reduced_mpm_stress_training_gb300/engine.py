@@ -155,6 +155,7 @@ class MPMEngine:
         self.chunk_size = chunk_size
         self.on_error = "raise"
         self._pending = None
+        self.surrogate = None
         self._allocate(fresh=True)
 
     # ------------------------------------------------------------------ layout
@@ -263,15 +264,31 @@ class MPMEngine:
         return gm, gvin, gvout
 
     # ------------------------------------------------------------------ stepping
+    def set_stress_surrogate(self, surrogate) -> None:
+        """Route the return map + stress of sand particles through a trained
+        ``surrogate.StressSurrogate`` (None restores the SVD path)."""
+        if surrogate is not None:
+            surrogate.bind(self)
+        self.surrogate = surrogate
+
+    def _p2g2p(self, time: float, dt: float) -> None:
+        sur = self.surrogate
+        if sur is None:
+            A.check(self.lib.mpm_p2g2p(C.byref(self.buf), time, dt, self.stream), "mpm_p2g2p")
+        else:
+            A.check(self.lib.mpm_p2g2p_surrogate(C.byref(self.buf), sur.params_ptr(), C.byref(sur.cfg),
+                                                 sur.fallback.data_ptr(), sur.stats.data_ptr(), time,
+                                                 dt, self.stream), "mpm_p2g2p_surrogate")
+
     def substep(self, time: float, dt: float) -> None:
         self.poll_status()
-        A.check(self.lib.mpm_p2g2p(C.byref(self.buf), time, dt, self.stream), "mpm_p2g2p")
+        self._p2g2p(time, dt)
         self._queue_status()
 
     def substep_raw(self, time: float, dt: float) -> None:
         """One substep without the lazy status bookkeeping (safe inside a
         CUDA-graph capture)."""
-        A.check(self.lib.mpm_p2g2p(C.byref(self.buf), time, dt, self.stream), "mpm_p2g2p")
+        self._p2g2p(time, dt)
 
     def graph(self, n_substeps: int, time: float, dt: float) -> "SubstepGraph":
         """Capture n_substeps substeps in one CUDA graph (see SubstepGraph)."""

@@ -110,6 +110,17 @@ class MPMSimulator:
         self.mpm_state = _State(self)
 
     @property
+    def engine(self) -> MPMEngine:
+        """The device engine (buffers and C-ABI driver) behind this simulator."""
+        return self._engine
+
+    def set_stress_surrogate(self, surrogate) -> None:
+        """Take the sand return map + stress of each p2g2p from a trained
+        ``surrogate.StressSurrogate`` (gated, SVD fallback); None restores
+        the plain path."""
+        self._engine.set_stress_surrogate(surrogate)
+
+    @property
     def on_error(self) -> str:
         return self._engine.on_error
 

@@ -12,6 +12,8 @@ stored as ``[xx, xy, xz, yy, yz, zz]`` (engine_stress/mpm_solver_warp.py:383).
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 import torch
 
@@ -141,3 +143,225 @@ class StressMLP:
         loss = self.loss_and_grad(x, target)
         self.adam(lr)
         return loss
+
+
+# ---------------------------------------------------------------------------
+# Gate configuration and the in-step surrogate
+# ---------------------------------------------------------------------------
+# rho_min: below |F F^T - I| = 1e-4 the float32 F (and so the plain return
+# map's stress, the training label) carries more than 1e-3 relative rounding
+# noise in the strain; those particles keep the SVD path.
+DEFAULT_CONFIG = dict(tol=1e-2, rho_min=1e-4, rho_max=2.5, nu_min=0.25, nu_max=0.35,
+                      phi_min=20.0, phi_max=40.0, dgamma_max=0.1)
+
+OUTCOMES = ("elastic", "plastic", "fb_domain", "fb_apex", "fb_step", "fb_gate", "fb_material")
+
+
+def make_config(**kw) -> A.MpmSurrogateConfig:
+    d = dict(DEFAULT_CONFIG)
+    unknown = set(kw) - set(d)
+    if unknown:
+        raise ValueError(f"unknown surrogate settings {sorted(unknown)}")
+    d.update(kw)
+    return A.MpmSurrogateConfig(**{k: float(v) for k, v in d.items()})
+
+
+def sand_scene(E: float, nu: float, friction_angle: float) -> A.MpmScene:
+    """A sand MpmScene carrying only the material (for the element kernels)."""
+    from .engine import dp_alpha, lame_from_E_nu
+
+    s = A.MpmScene()
+    mu, lam = lame_from_E_nu(E, nu)
+    s.material = A.SAND
+    s.mu, s.lam, s.alpha = mu, lam, dp_alpha(friction_angle)
+    s.n_grid, s.dx, s.inv_dx = 1, 1.0, 1.0
+    return s
+
+
+class StressSurrogate:
+    """A trained network plus its gate settings, attached to an engine with
+    ``MPMEngine.set_stress_surrogate``: each substep then runs
+    ``mpm_p2g2p_surrogate`` (network stress for sand particles that pass the
+    gate, the SVD return map for the rest)."""
+
+    def __init__(self, net: StressMLP, **cfg):
+        self.net = net
+        self.cfg = make_config(**cfg)
+        self.fallback = None
+        self.stats = torch.zeros(A.SUR_STATS, dtype=torch.int32, device=net.device)
+
+    def params_ptr(self) -> int:
+        return self.net.params.data_ptr()
+
+    def bind(self, engine) -> None:
+        if engine.device != self.net.device:
+            raise ValueError("the network and the engine must be on the same device")
+        n = max(engine.n_particles, 1)
+        if self.fallback is None or self.fallback.numel() < 2 * n:
+            self.fallback = torch.empty(2 * n, dtype=torch.int32, device=self.net.device)
+
+    def reset_stats(self) -> None:
+        self.stats.zero_()
+
+    def outcome_counts(self) -> dict:
+        s = self.stats.cpu().tolist()
+        return {name: s[i] for i, name in enumerate(OUTCOMES)}
+
+    def apply(self, F_trial: torch.Tensor, E: float, nu: float, friction_angle: float):
+        """Element form (mpm_surrogate_apply): F_trial (n,9) -> F (n,9), stress (n,9), codes (n)."""
+        F_trial = F_trial.to(self.net.device, torch.float32).reshape(-1, 9).contiguous()
+        n = F_trial.shape[0]
+        Fo = torch.empty_like(F_trial)
+        tau = torch.empty_like(F_trial)
+        codes = torch.empty(n, dtype=torch.int32, device=self.net.device)
+        sc = sand_scene(E, nu, friction_angle)
+        A.check(self.net.lib.mpm_surrogate_apply(C.byref(sc), self.params_ptr(), C.byref(self.cfg),
+                                                 F_trial.data_ptr(), Fo.data_ptr(), tau.data_ptr(),
+                                                 codes.data_ptr(), n, _stream(self.net.device)),
+                "mpm_surrogate_apply")
+        return Fo, tau, codes
+
+
+# ---------------------------------------------------------------------------
+# Training tuples (F_trial, material) -> stress of the plain return map
+# ---------------------------------------------------------------------------
+def haar_rotations(n: int, rng: np.random.Generator) -> np.ndarray:
+    """n Haar-random rotations (QR of Gaussian matrices, signs fixed, det +1)."""
+    q, r = np.linalg.qr(rng.standard_normal((n, 3, 3)))
+    q = q * np.sign(np.diagonal(r, axis1=1, axis2=2))[:, None, :]
+    flip = np.linalg.det(q) < 0
+    q[flip, :, 0] *= -1.0
+    return q
+
+
+def synthetic_F(n: int, rng: np.random.Generator, max_log: float = 0.3,
+                log_uniform_scale: bool = False, min_log: float = 4e-5) -> np.ndarray:
+    """F = R diag(exp(s)) Q^T with Haar R, Q.  s ~ U(-max_log, max_log)^3, or
+    (log_uniform_scale) s = m u with u a random unit direction and m
+    log-uniform in [min_log, max_log], which covers the small strains of a
+    settling column."""
+    if log_uniform_scale:
+        u = rng.standard_normal((n, 3))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        m = np.exp(rng.uniform(np.log(min_log), np.log(max_log), size=(n, 1)))
+        s = u * m
+    else:
+        s = rng.uniform(-max_log, max_log, size=(n, 3))
+    R = haar_rotations(n, rng)
+    Q = haar_rotations(n, rng)
+    F = (R * np.exp(s)[:, None, :]) @ Q.transpose(0, 2, 1)
+    return F.reshape(n, 9).astype(np.float32)
+
+
+def rollout_F_trial(scene, n_substeps: int, every: int, device="cuda:0") -> torch.Tensor:
+    """F_trial = (I + dt C) F of every particle, sampled every ``every``
+    substeps of a plain-solver rollout of ``scene`` (scenarios.Scene)."""
+    from .scenarios import build_simulator
+
+    sim = build_simulator(scene, device=device)
+    out = []
+    eye = torch.eye(3, device=device)
+    for k in range(1, n_substeps + 1):
+        sim.p2g2p(k, scene.dt)
+        if k % every == 0:
+            F = sim.engine.export(A.FIELD_F).reshape(-1, 3, 3)
+            Cm = sim.engine.export(A.FIELD_C).reshape(-1, 3, 3)
+            out.append(((eye + scene.dt * Cm) @ F).reshape(-1, 9))
+    return torch.cat(out)
+
+
+def label(F_trial: torch.Tensor, E: float, nu: float, friction_angle: float):
+    """Network inputs x (n,12) and targets y (n,6) of one material, labelled by
+    the plain return map (mpm_return_map) and mpm_surrogate_features."""
+    lib = A.load()
+    F_trial = F_trial.to(torch.float32).reshape(-1, 9).contiguous()
+    dev = F_trial.device
+    n = F_trial.shape[0]
+    sc = sand_scene(E, nu, friction_angle)
+    Fo = torch.empty_like(F_trial)
+    tau = torch.empty_like(F_trial)
+    st = _stream(dev)
+    A.check(lib.mpm_return_map(C.byref(sc), F_trial.data_ptr(), None, Fo.data_ptr(), tau.data_ptr(),
+                               n, st), "mpm_return_map")
+    x = torch.empty(n, IN, dtype=torch.float32, device=dev)
+    y = torch.empty(n, OUT, dtype=torch.float32, device=dev)
+    A.check(lib.mpm_surrogate_features(C.byref(sc), F_trial.data_ptr(), tau.data_ptr(), x.data_ptr(),
+                                       y.data_ptr(), n, st), "mpm_surrogate_features")
+    return x, y
+
+
+def sample_materials(n_groups: int, rng: np.random.Generator):
+    """(E, nu, friction angle) per group: E log-uniform [1e5, 1e6] Pa,
+    nu U(0.25, 0.35), friction angle U(20, 40) degrees."""
+    E = np.exp(rng.uniform(np.log(1e5), np.log(1e6), n_groups))
+    nu = rng.uniform(0.25, 0.35, n_groups)
+    phi = rng.uniform(20.0, 40.0, n_groups)
+    return list(zip(E.tolist(), nu.tolist(), phi.tolist()))
+
+
+def build_training_set(n_total: int, device="cuda:0", seed: int = 0, rollout: torch.Tensor | None = None,
+                       group: int = 65536, rho_min: float = DEFAULT_CONFIG["rho_min"]):
+    """About n_total tuples: 40 % F = R diag(exp s) with s ~ U(-0.3, 0.3),
+    30 % the same with log-uniform strain magnitude, 30 % rollout F_trial
+    (when given; otherwise more of the first two).  Every group of ``group``
+    tuples is labelled with its own sampled material.  Tuples with
+    |F F^T - I| < rho_min (outside the gate's domain, labels dominated by
+    float32 rounding) are dropped."""
+    rng = np.random.default_rng(seed)
+    n_roll = int(0.3 * n_total) if rollout is not None and rollout.shape[0] > 0 else 0
+    n_syn = n_total - n_roll
+    n_uni = int(round(n_syn * 4 / 7))
+    Fs = [torch.from_numpy(synthetic_F(n_uni, rng)),
+          torch.from_numpy(synthetic_F(n_syn - n_uni, rng, log_uniform_scale=True))]
+    Fs = [f.to(device) for f in Fs]
+    if n_roll:
+        pick = torch.from_numpy(rng.choice(rollout.shape[0], n_roll, replace=n_roll > rollout.shape[0]))
+        Fs.append(rollout[pick.to(rollout.device)].to(device))
+    F = torch.cat(Fs)
+    F = F[torch.from_numpy(rng.permutation(F.shape[0])).to(device)]
+    xs, ys = [], []
+    mats = sample_materials((n_total + group - 1) // group, rng)
+    x9_min = (np.log10(rho_min) + 2.5) / 1.5  # the log-strain input at rho_min
+    for g, (E, nu, phi) in enumerate(mats):
+        x, y = label(F[g * group:(g + 1) * group], E, nu, phi)
+        keep = x[:, 9] >= x9_min
+        xs.append(x[keep])
+        ys.append(y[keep])
+    return torch.cat(xs), torch.cat(ys)
+
+
+def train(net: StressMLP, x: torch.Tensor, y: torch.Tensor, steps: int, batch: int = 65536,
+          lr: float = 1e-3, lr_min: float = 1e-5, seed: int = 0, log_every: int = 0) -> list:
+    """Adam with a cosine decay from lr to lr_min over ``steps`` minibatches
+    drawn from shuffled epochs of (x, y); returns the logged (step, loss)."""
+    gen = torch.Generator(device=x.device)
+    gen.manual_seed(seed)
+    n = x.shape[0]
+    batch = min(batch, n)
+    perm = torch.randperm(n, generator=gen, device=x.device)
+    pos = 0
+    log = []
+    for s in range(steps):
+        if pos + batch > n:
+            perm = torch.randperm(n, generator=gen, device=x.device)
+            pos = 0
+        idx = perm[pos:pos + batch]
+        pos += batch
+        cur = lr_min + 0.5 * (lr - lr_min) * (1.0 + np.cos(np.pi * s / max(steps - 1, 1)))
+        loss = net.loss_and_grad(x[idx], y[idx])
+        net.adam(cur)
+        if log_every and (s % log_every == 0 or s == steps - 1):
+            log.append((s, float(loss.item())))
+    return log
+
+
+def stress_errors(tau: torch.Tensor, tau_ref: torch.Tensor) -> dict:
+    """Relative L2 over all rows and the per-row relative error quantiles."""
+    d = (tau - tau_ref).double()
+    r = tau_ref.double()
+    rn = r.norm(dim=1)
+    row = d.norm(dim=1) / rn.clamp_min(1e-30)
+    ok = rn > 0
+    q = torch.quantile(row[ok][:1_000_000].float(), torch.tensor([0.5, 0.99, 1.0], device=row.device))
+    return {"rel_l2": float(d.norm() / r.norm().clamp_min(1e-30)), "row_p50": float(q[0]),
+            "row_p99": float(q[1]), "row_max": float(q[2])}
