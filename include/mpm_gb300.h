@@ -312,6 +312,31 @@ int mpm_g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogateC
 int mpm_p2g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogateConfig *cfg,
                         void *fallback, int32_t *stats, float time, float dt, void *stream);
 
+/* ---- reverse mode (sand) ---------------------------------------------
+ * No counterpart in the reference (it has no wp.Tape or gradient code):
+ * the adjoint of one substep, the latest substep first.  Call it with the
+ * live state holding the state BEFORE the substep, after mpm_sort, mpm_p2g
+ * and mpm_grid_update have run on that state with the substep's time and
+ * dt (the grid of the substep is then in the workspace).  adj_out is the
+ * adjoint of the state after the substep, adj_in receives the adjoint of
+ * the state before it; both hold MPM_ADJ_WORDS floats per particle in user
+ * order: x 0-2, v 3-5, C 6-14, F 15-23, stress 24-32 (matrices row-major).
+ * grid_adj: device scratch of plan.total_blocks * 64 * 16 bytes.
+ * theta_bar: 3 device doubles, the adjoints of (mu, lam, alpha), added to.
+ * Scenes must be sand.  Particles outside the grid pass their adjoint
+ * through unchanged (the forward carries them over). */
+#define MPM_ADJ_WORDS 36
+int mpm_adjoint_substep(MpmBuffers *b, const float *adj_out, float *adj_in, void *grid_adj,
+                        double *theta_bar, float time, float dt, void *stream);
+
+/* Element form of the return-map adjoint (sand): F_trial (n,9) and the
+ * adjoints of the returned F and of the stress (n,9 each) -> the adjoint of
+ * F_trial (n,9, written) and of (mu, lam, alpha) (3 device doubles, added
+ * to).  The return map it differentiates is mpm_return_map's. */
+int mpm_return_map_vjp(const MpmScene *scene, const float *F_trial, const float *F_bar,
+                       const float *stress_bar, float *F_trial_bar, double *theta_bar, int64_t n,
+                       void *stream);
+
 /* ---- misc ------------------------------------------------------------ */
 int mpm_abi_version(void);
 /* sizeof of the ABI structs, for binding checks: out[0..3] =

@@ -68,6 +68,8 @@ class MpmSurrogateConfig(C.Structure):
 (SUR_ELASTIC, SUR_PLASTIC, SUR_FB_DOMAIN, SUR_FB_APEX, SUR_FB_STEP, SUR_FB_GATE,
  SUR_FB_MATERIAL, SUR_LAST_FALLBACKS) = range(8)
 SUR_STATS = 8
+ADJ_WORDS = 36
+ADJ_X, ADJ_V, ADJ_C, ADJ_F, ADJ_STRESS = 0, 3, 6, 15, 24
 
 
 class MPMLibraryError(RuntimeError):
@@ -107,6 +109,10 @@ _SIGS = {
                            C.c_void_p, C.c_void_p, C.c_float, C.c_void_p], C.c_int),
     "mpm_p2g2p_surrogate": ([C.POINTER(MpmBuffers), C.c_void_p, C.POINTER(MpmSurrogateConfig),
                              C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
+    "mpm_adjoint_substep": ([C.POINTER(MpmBuffers), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                             C.c_float, C.c_float, C.c_void_p], C.c_int),
+    "mpm_return_map_vjp": ([C.POINTER(MpmScene), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                            C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
     "mpm_abi_version": ([], C.c_int),
     "mpm_struct_sizes": ([C.POINTER(C.c_int64)], None),
     "mpm_error_string": ([C.c_int], C.c_char_p),

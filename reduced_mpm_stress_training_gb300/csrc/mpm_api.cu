@@ -339,6 +339,26 @@ int mpm_p2g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogat
     return mpm_g2p_surrogate(b, mlp_params, cfg, fallback, stats, dt, stream);
 }
 
+int mpm_adjoint_substep(MpmBuffers *b, const float *adj_out, float *adj_in, void *grid_adj, double *theta_bar,
+                        float time, float dt, void *stream) {
+    if (!buffers_ok(b) || !theta_bar || !grid_adj) return MPM_ERR_ARG;
+    if (b->plan.n_particles > 0 && (!adj_out || !adj_in || adj_out == adj_in)) return MPM_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(grid_adj) & 15) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_adjoint(make_ctx(b, stream, b->cur), adj_out, adj_in, static_cast<float4 *>(grid_adj),
+                                  theta_bar, time, dt));
+    return MPM_OK;
+}
+
+int mpm_return_map_vjp(const MpmScene *scene, const float *F_trial, const float *F_bar, const float *stress_bar,
+                       float *F_trial_bar, double *theta_bar, int64_t n, void *stream) {
+    if (!scene || !theta_bar || n < 0) return MPM_ERR_ARG;
+    if (n > 0 && (!F_trial || !F_bar || !stress_bar || !F_trial_bar)) return MPM_ERR_ARG;
+    if (scene->material != MPM_SAND) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_return_map_vjp(*scene, F_trial, F_bar, stress_bar, F_trial_bar, theta_bar, n,
+                                         static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
 int mpm_export_grid(MpmBuffers *b, int32_t scene, float *grid_m, float *grid_v_in,
                     float *grid_v_out, void *stream) {
     if (!buffers_ok(b) || scene < 0 || scene >= b->plan.n_scenes) return MPM_ERR_ARG;

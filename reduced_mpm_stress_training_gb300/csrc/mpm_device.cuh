@@ -128,6 +128,15 @@ __device__ __forceinline__ int64_t node_addr(int64_t block_begin, int nb, int ix
     return blk * kBlockNodes + (((ix & 3) << 4) | ((iy & 3) << 2) | (iz & 3));
 }
 
+// block coordinates (per axis, in blocks) of a global grid block of scene S
+__device__ __forceinline__ void chunk_block(const MpmScene &S, int gblock, int &bx, int &by, int &bz) {
+    const int nb = S.n_blocks_axis;
+    int lb = (int)(gblock - S.block_begin);
+    bz = lb % nb;
+    by = (lb / nb) % nb;
+    bx = lb / (nb * nb);
+}
+
 // scene owning a global grid block / a user-order particle (binary search)
 __device__ __forceinline__ int scene_of_block(const MpmScene *sc, int n_scenes, int64_t blk) {
     int lo = 0, hi = n_scenes - 1;

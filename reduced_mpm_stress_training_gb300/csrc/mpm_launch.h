@@ -39,6 +39,11 @@ cudaError_t launch_surrogate(const Ctx &cx, const void *mlp_params, const MpmSur
 cudaError_t launch_surrogate_apply(const MpmScene &scene, const void *mlp_params, const MpmSurrogateConfig &cfg,
                                    const float *F, float *Fo, float *tau, int *codes, int64_t n, int num_sms,
                                    cudaStream_t stream);
+// reverse mode of one substep (mpm_adjoint.cu); see mpm_adjoint_substep
+cudaError_t launch_adjoint(const Ctx &cx, const float *adj_out, float *adj_in, float4 *grid_adj, double *thb,
+                           float time, float dt);
+cudaError_t launch_return_map_vjp(const MpmScene &scene, const float *Ft, const float *Fb, const float *Tb,
+                                  float *Ftb, double *thb, int64_t n, cudaStream_t st);
 cudaError_t launch_features(const MpmScene &scene, const float *F, const float *stress, float *x, float *y,
                             int64_t n, cudaStream_t stream);
 

@@ -26,15 +26,6 @@
 
 namespace mpm {
 
-__device__ __forceinline__ void chunk_block(const MpmScene &S, int gblock, int &bx, int &by,
-                                            int &bz) {
-    const int nb = S.n_blocks_axis;
-    int lb = (int)(gblock - S.block_begin);
-    bz = lb % nb;
-    by = (lb / nb) % nb;
-    bx = lb / (nb * nb);
-}
-
 // ---------------------------------------------------------------------------
 // P2G: p2g_apic_stress_given, engine_stress/mpm_utils.py:190-227
 //   grid_v_in += (w m)(v + C dpos) + dt (-vol tau) grad w,  grid_m += w m

@@ -308,6 +308,27 @@ class MPMEngine:
         else:
             raise ValueError(name)
 
+    # ------------------------------------------------------------------ checkpoints
+    def reinit(self) -> None:
+        """Back to the freshly initialised state (mpm_init: zero state, F = I,
+        identity order); the caller reloads the particle fields."""
+        A.check(self.lib.mpm_init(C.byref(self.buf), self.stream), "mpm_init")
+
+    def snapshot(self) -> tuple:
+        """Device copy of the live particle state (records and cell keys) with
+        the host-side control needed to resume from it."""
+        b = self.buf
+        return (self._state[b.cur].clone(), int(b.cur), int(b.substep))
+
+    def restore(self, snap: tuple) -> None:
+        """Resume from a snapshot (the grid is rebuilt by the next substep)."""
+        data, cur, substep = snap
+        b = self.buf
+        self._state[cur].copy_(data)
+        b.cur = cur
+        b.substep = substep
+        b.keys_valid = 0  # the workspace histograms belong to another state
+
     # ------------------------------------------------------------------ status
     def _queue_status(self) -> None:
         self._status_host.copy_(self._status, non_blocking=True)
