@@ -57,7 +57,141 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="sand_column_1m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint measurement")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-stress measurement")
     return ap.parse_args()
+
+
+def _events_ms(fn, reps: int) -> float:
+    """Mean milliseconds of fn() over reps calls, CUDA events on the current stream."""
+    import torch
+
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        fn()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def adjoint_extra(device) -> dict:
+    """Differentiable rollout (131,072 sand particles, 96^3, 100 substeps, dt
+    1e-4, v0 ~ N(0, 0.1^2)): forward time, forward + hand-written adjoint
+    time (checkpoints every 10 substeps, recomputed), and the gradients of
+    the MSE to a target rollout (E = 3e5, friction 35 deg) against central
+    differences of the float32 forward."""
+    import torch
+
+    from reduced_mpm_stress_training_gb300 import scenarios as S
+    from reduced_mpm_stress_training_gb300.adjoint import SandRollout
+
+    sc = S.sand_rollout_131k()
+    sand = SandRollout(sc, checkpoint_every=10, device=device)
+    v0 = sand.v0_default
+    target = sand.positions(sand.forward(v0, 3e5, 35.0, keep=False)).clone()
+    E, phi = sc.E, sc.friction_angle
+
+    def fwd():
+        sand.forward(v0, E, phi, keep=False)
+
+    state = {}
+
+    def fwd_adj():
+        x = sand.positions(sand.forward(v0, E, phi, keep=True))
+        state["g"] = sand.backward(2.0 * (x - target) / x.numel())
+
+    fwd()
+    fwd_adj()
+    t_f = _events_ms(fwd, 3)
+    t_fa = _events_ms(fwd_adj, 3)
+    v0b, Eb, phib = state["g"]
+
+    def J(v, e_, p_):
+        x = sand.positions(sand.forward(v, e_, p_, keep=False))
+        return float(((x - target) ** 2).mean())
+
+    rh = 1e-2
+    checks = {"E": (Eb, (J(v0, E * (1 + rh), phi) - J(v0, E * (1 - rh), phi)) / (2 * rh * E)),
+              "friction_angle": (phib, (J(v0, E, phi * (1 + rh)) - J(v0, E, phi * (1 - rh))) / (2 * rh * phi))}
+    g = torch.Generator(device=device).manual_seed(0)
+    for d in range(4):
+        dirn = torch.randn(v0.shape, generator=g, device=device)
+        dirn /= dirn.norm()
+        h = rh * v0.norm().item()
+        fd = (J(v0 + h * dirn, E, phi) - J(v0 - h * dirn, E, phi)) / (2 * h)
+        checks[f"v0_direction_{d}"] = (float((v0b.double() * dirn.double()).sum()), fd)
+    return {"workload": f"sand_rollout_131k: {sc.n_particles} particles, {sc.n_grid}^3 grid, "
+                        f"{sc.substeps} substeps, dt {sc.dt}, checkpoints every 10",
+            "forward_ms": round(t_f, 3), "forward_adjoint_ms": round(t_fa, 3),
+            "ratio": round(t_fa / t_f, 3),
+            "fd_relative_step": rh,
+            "gradient_vs_fd": {k: {"adjoint": a, "fd": f, "rel_err": abs(a - f) / abs(f)}
+                               for k, (a, f) in checks.items()}}
+
+
+def surrogate_extra(device) -> dict:
+    """Learned stress: the network trained by the library's kernels (8M
+    tuples, Adam lr 1e-3, batch 65,536, 60,000 steps), then the 1M sand
+    column substep with the surrogate stress stage against the plain
+    return-map substep, from the same state after 2,000 plain substeps."""
+    import torch
+
+    from reduced_mpm_stress_training_gb300 import _capi as A
+    from reduced_mpm_stress_training_gb300 import scenarios as S
+    from reduced_mpm_stress_training_gb300 import surrogate as SU
+
+    t0 = time.perf_counter()
+    roll = SU.rollout_F_trial(S.sand_column_32k(), 600, 60, device=device)
+    x, y = SU.build_training_set(8_000_000, device=device, seed=0, rollout=roll)
+    net = SU.StressMLP(device, seed=0)
+    t1 = time.perf_counter()
+    log = SU.train(net, x, y, steps=60000, batch=65536, lr=1e-3, lr_min=1e-5, log_every=20000)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t1
+    del x, y
+    sc = S.sand_column_1m()
+    sim = S.build_simulator(sc, device=device)
+    eng = sim.engine
+    for k in range(2):
+        sim.p2g2p(k, sc.dt)
+    g = eng.graph(200, 0.0, sc.dt)
+    for _ in range(10):
+        g.replay()
+    torch.cuda.synchronize()
+    snap = eng.snapshot()
+    eng.restore(snap)
+    eng.substep_raw(0.0, sc.dt)
+    tau_plain = eng.export(A.FIELD_STRESS).reshape(-1, 9).clone()
+    sur = SU.StressSurrogate(net)
+    eng.set_stress_surrogate(sur)
+    eng.restore(snap)
+    eng.substep_raw(0.0, sc.dt)
+    tau_sur = eng.export(A.FIELD_STRESS).reshape(-1, 9).clone()
+    counts = sur.outcome_counts()
+    err = SU.stress_errors(tau_sur, tau_plain)
+
+    def timed(surrogate):
+        eng.set_stress_surrogate(surrogate)
+        eng.restore(snap)
+        eng.substep_raw(0.0, sc.dt)
+        gg = eng.graph(20, 0.0, sc.dt)
+        gg.replay()
+        return _events_ms(gg.replay, 3) / 20
+
+    t_sur = timed(sur)
+    t_plain = timed(None)
+    n = sc.n_particles
+    acc = counts["elastic"] + counts["plastic"]
+    return {"workload": "sand_column_1m after 2,002 plain substeps (settling column)",
+            "plain_step_ms": round(t_plain, 4), "surrogate_step_ms": round(t_sur, 4),
+            "surrogate_over_plain": round(t_sur / t_plain, 3),
+            "stress_rel_l2_vs_plain": err["rel_l2"],
+            "accepted_fraction": acc / n, "outcomes": counts,
+            "training": {"tuples": 8_000_000, "steps": 60000, "batch": 65536, "seconds": round(t_train, 1),
+                         "data_seconds": round(t1 - t0, 1), "loss": log[-1][1]}}
 
 
 def dist_env():
@@ -357,6 +491,10 @@ def gb300_arm(args, sc, world, rank, local):
         "clocks": clk,
         "status": status,
     }
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_extra(device)
+    if not args.no_surrogate:
+        line["surrogate"] = surrogate_extra(device)
     if not args.no_cpu_baseline:
         rate, nt, done, el = cpu_port_rate(sc, sc.n_particles, 10.0, 30)
         line["cpu_baseline"] = {"value": rate, "unit": "particle-substeps/s", "cores": nt,
