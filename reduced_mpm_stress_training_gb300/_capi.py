@@ -111,6 +111,10 @@ _SIGS = {
                              C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "mpm_adjoint_substep": ([C.POINTER(MpmBuffers), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                              C.c_float, C.c_float, C.c_void_p], C.c_int),
+    "mpm_substep_grid_bytes": ([C.POINTER(MpmPlan)], C.c_int64),
+    "mpm_save_substep_grid": ([C.POINTER(MpmBuffers), C.c_void_p, C.c_void_p], C.c_int),
+    "mpm_load_substep_grid": ([C.POINTER(MpmBuffers), C.c_void_p, C.c_void_p], C.c_int),
+    "mpm_clear_grid": ([C.POINTER(MpmBuffers), C.c_void_p], C.c_int),
     "mpm_return_map_vjp": ([C.POINTER(MpmScene), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                             C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
     "mpm_abi_version": ([], C.c_int),

@@ -48,7 +48,7 @@ class SandRollout:
             raise ValueError("checkpoint_every must be >= 1")
         self.scene = scene
         self.n_substeps = int(n_substeps if n_substeps is not None else scene.substeps)
-        self.k = int(checkpoint_every)
+        self._k = 0
         self.dt = float(scene.dt)
         self.device = torch.device(device)
         self.params = scene_params(scene)
@@ -68,9 +68,33 @@ class SandRollout:
         self.grid_adj = torch.empty(self.engine.plan.total_blocks * 64 * 4, dtype=torch.float32, device=dev)
         self.theta_bar = torch.zeros(3, dtype=torch.float64, device=dev)
         self.adj = [torch.zeros(self.n * A.ADJ_WORDS, dtype=torch.float32, device=dev) for _ in range(2)]
-        self.checkpoints: list = []
+        self.k = int(checkpoint_every)
         self.E = float(scene.E)
         self.friction_angle = float(scene.friction_angle)
+
+    @property
+    def k(self) -> int:
+        """Checkpoint interval (substeps per recomputed segment)."""
+        return self._k
+
+    @k.setter
+    def k(self, k: int) -> None:
+        """Allocate the checkpoint storage: one state buffer per checkpoint,
+        k + 1 state buffers for a recomputed segment, k saved grids."""
+        k = int(k)
+        if k < 1:
+            raise ValueError("checkpoint interval must be >= 1")
+        if k == self._k:
+            return
+        dev = self.device
+        sb = self.engine.plan.state_bytes
+        gb = self.lib.mpm_substep_grid_bytes(C.byref(self.engine.plan))
+        n_ckpt = (self.n_substeps + k - 1) // k
+        self.checkpoints = [torch.empty(sb, dtype=torch.uint8, device=dev) for _ in range(n_ckpt)]
+        self.pool = [torch.empty(sb, dtype=torch.uint8, device=dev) for _ in range(k + 1)]
+        self.grids = [torch.empty(gb, dtype=torch.uint8, device=dev) for _ in range(k)]
+        self.have_checkpoints = False
+        self._k = k
 
     # ------------------------------------------------------------------ forward
     def set_material(self, E: float, friction_angle: float) -> None:
@@ -99,11 +123,13 @@ class SandRollout:
         self.set_material(E, friction_angle)
         self._start(v0.detach().to(self.device, torch.float32).reshape(self.n, 3))
         e = self.engine
-        self.checkpoints = []
+        b = e.buf
+        self.have_checkpoints = False
         for step in range(self.n_substeps):
             if keep and step % self.k == 0:
-                self.checkpoints.append(e.snapshot())
+                self.checkpoints[step // self.k].copy_(e._state[b.cur])
             e.substep_raw(self.time_of(step), self.dt)
+        self.have_checkpoints = keep
         return e.export(A.FIELD_U).reshape(self.n, 3)
 
     def positions(self, u: torch.Tensor) -> torch.Tensor:
@@ -111,25 +137,25 @@ class SandRollout:
         return self.x0.double() + u.double()
 
     # ------------------------------------------------------------------ reverse
-    def _adjoint_substep(self, step: int, adj_out: torch.Tensor, adj_in: torch.Tensor) -> None:
-        e = self.engine
-        t = self.time_of(step)
-        e.stage("sort")
-        e.stage("p2g", dt=self.dt)
-        e.stage("grid", time=t, dt=self.dt)
-        A.check(self.lib.mpm_adjoint_substep(C.byref(e.buf), adj_out.data_ptr(), adj_in.data_ptr(),
-                                             self.grid_adj.data_ptr(), self.theta_bar.data_ptr(), t,
-                                             self.dt, _stream(self.device)), "mpm_adjoint_substep")
+    def _call(self, name: str, *args) -> None:
+        A.check(getattr(self.lib, name)(C.byref(self.engine.buf), *args, _stream(self.device)), name)
 
     def backward(self, x_bar: torch.Tensor):
         """Adjoints (v0 (n,3), E, friction angle) of <x_bar, x_final> (x_bar is
         also the adjoint of the final displacement).  x_bar may instead be a
         full (n, 36) seed on the final state (x, v, C, F, stress words as in
         mpm_adjoint_substep).  The adjoint of the whole initial state is left
-        in ``state_bar`` (n, 36)."""
-        if not self.checkpoints:
+        in ``state_bar`` (n, 36).
+
+        Per segment (newest first): the segment's states are recomputed from
+        its checkpoint straight into ``pool`` (G2P writes each new state into
+        the next pool buffer: no copies), each substep's grid is saved after
+        its grid update, then the substeps are reversed newest first from
+        their pool state and saved grid."""
+        if not self.have_checkpoints:
             raise RuntimeError("run forward(keep=True) first")
         e = self.engine
+        b = e.buf
         out, inp = self.adj
         out.zero_()
         seed = x_bar.to(self.device, torch.float32)
@@ -138,20 +164,39 @@ class SandRollout:
         else:
             out.view(self.n, A.ADJ_WORDS)[:, A.ADJ_X:A.ADJ_X + 3] = seed.reshape(self.n, 3)
         self.theta_bar.zero_()
-        for seg in reversed(range(len(self.checkpoints))):
-            start = seg * self.k
-            stop = min(start + self.k, self.n_substeps)
-            e.restore(self.checkpoints[seg])
-            states = []
-            for step in range(start, stop):
-                states.append(e.snapshot())
-                if step + 1 < stop:
-                    e.substep_raw(self.time_of(step), self.dt)
-            for step in reversed(range(start, stop)):
-                e.restore(states[step - start])
-                self._adjoint_substep(step, out, inp)
-                out, inp = inp, out
-            del states
+        own = (b.state[0], b.state[1])
+        cur0, substep0 = b.cur, b.substep
+        try:
+            for seg in reversed(range(len(self.checkpoints))):
+                start = seg * self.k
+                L = min(self.k, self.n_substeps - start)
+                self.pool[0].copy_(self.checkpoints[seg])
+                b.state[b.cur] = self.pool[0].data_ptr()
+                b.keys_valid = 0
+                self._call("mpm_clear_grid")
+                for j in range(L):
+                    t = self.time_of(start + j)
+                    if j + 1 < L:
+                        b.state[b.cur ^ 1] = self.pool[j + 1].data_ptr()
+                    e.stage("sort")
+                    e.stage("p2g", dt=self.dt)
+                    e.stage("grid", time=t, dt=self.dt)
+                    self._call("mpm_save_substep_grid", self.grids[j].data_ptr())
+                    if j + 1 < L:
+                        e.stage("g2p", dt=self.dt)
+                for j in reversed(range(L)):
+                    b.state[b.cur] = self.pool[j].data_ptr()
+                    self._call("mpm_load_substep_grid", self.grids[j].data_ptr())
+                    A.check(self.lib.mpm_adjoint_substep(C.byref(b), out.data_ptr(), inp.data_ptr(),
+                                                         self.grid_adj.data_ptr(), self.theta_bar.data_ptr(),
+                                                         self.time_of(start + j), self.dt, _stream(self.device)),
+                            "mpm_adjoint_substep")
+                    out, inp = inp, out
+        finally:
+            b.state[0], b.state[1] = own
+            b.cur, b.substep = cur0, substep0
+            b.keys_valid = 0
+            self._call("mpm_clear_grid")
         self.state_bar = out.view(self.n, A.ADJ_WORDS).clone()
         v0_bar = self.state_bar[:, A.ADJ_V:A.ADJ_V + 3].clone()
         mu_b, lam_b, alpha_b = (float(x) for x in self.theta_bar.cpu())

@@ -349,6 +349,29 @@ int mpm_adjoint_substep(MpmBuffers *b, const float *adj_out, float *adj_in, void
     return MPM_OK;
 }
 
+int64_t mpm_substep_grid_bytes(const MpmPlan *plan) {
+    if (!plan) return -1;
+    return mpm::substep_grid_bytes(plan->total_blocks, plan->n_particles);
+}
+
+int mpm_save_substep_grid(MpmBuffers *b, void *dst, void *stream) {
+    if (!buffers_ok(b) || !dst || (reinterpret_cast<uintptr_t>(dst) & 255)) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_save_grid(make_ctx(b, stream, b->cur), dst));
+    return MPM_OK;
+}
+
+int mpm_load_substep_grid(MpmBuffers *b, const void *src, void *stream) {
+    if (!buffers_ok(b) || !src || (reinterpret_cast<uintptr_t>(src) & 255)) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_load_grid(make_ctx(b, stream, b->cur), src));
+    return MPM_OK;
+}
+
+int mpm_clear_grid(MpmBuffers *b, void *stream) {
+    if (!buffers_ok(b)) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_clear_grid(make_ctx(b, stream, b->cur)));
+    return MPM_OK;
+}
+
 int mpm_return_map_vjp(const MpmScene *scene, const float *F_trial, const float *F_bar, const float *stress_bar,
                        float *F_trial_bar, double *theta_bar, int64_t n, void *stream) {
     if (!scene || !theta_bar || n < 0) return MPM_ERR_ARG;

@@ -44,6 +44,11 @@ cudaError_t launch_adjoint(const Ctx &cx, const float *adj_out, float *adj_in, f
                            float time, float dt);
 cudaError_t launch_return_map_vjp(const MpmScene &scene, const float *Ft, const float *Fb, const float *Tb,
                                   float *Ftb, double *thb, int64_t n, cudaStream_t st);
+// saved grids for the reverse pass (mpm_checkpoint.cu)
+int64_t substep_grid_bytes(int64_t total_blocks, int64_t n);
+cudaError_t launch_save_grid(const Ctx &cx, void *dst);
+cudaError_t launch_load_grid(const Ctx &cx, const void *src);
+cudaError_t launch_clear_grid(const Ctx &cx);
 cudaError_t launch_features(const MpmScene &scene, const float *F, const float *stress, float *x, float *y,
                             int64_t n, cudaStream_t stream);
 
