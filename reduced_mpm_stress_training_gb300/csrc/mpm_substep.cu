@@ -44,11 +44,13 @@ namespace mpm {
 // non-zero node into the global grid.
 // ---------------------------------------------------------------------------
 constexpr int kP2GWarps = 4;
-constexpr int kPassCap = 512;  // layer-major entries buffered per batch
+constexpr int kPassCap = 256;  // layer-major entries buffered per batch
+constexpr int kP2GQuads = 8;   // record quads P2G reads (q0-q7, 128 B)
 
 struct P2GWarpSmem {
     float4 tile[kTileNodes];
-    int perm[kPassCap];  // sorted positions (indices into order[])
+    int perm[kPassCap];                 // record slots of the batch, layer-major
+    float4 rec[kP2GQuads][32];          // records of the next 32-particle window
 };
 
 struct P2GParticle {
@@ -60,12 +62,10 @@ struct P2GParticle {
     float T[9];   // -dt vol inv_dx tau
 };
 
-__device__ __forceinline__ bool p2g_load(const MpmScene &S, const PState &st, int slot, int bx,
-                                         int by, int bz, float dt, P2GParticle &P) {
+__device__ __forceinline__ bool p2g_load(const MpmScene &S, const float4 (&q)[kP2GQuads], int bx, int by,
+                                         int bz, float dt, P2GParticle &P) {
     // record quads 0-7: x0 m | vol .. | u v.x | v.yz C0 C1 | C2-5 | C6-8 tau0 | tau1-4 | tau5-8
-    const float4 q0 = ldrec(st, slot, 0), q1 = ldrec(st, slot, 1), q2 = ldrec(st, slot, 2),
-                 q3 = ldrec(st, slot, 3), q4 = ldrec(st, slot, 4), q5 = ldrec(st, slot, 5),
-                 q6 = ldrec(st, slot, 6), q7 = ldrec(st, slot, 7);
+    const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3], q4 = q[4], q5 = q[5], q6 = q[6], q7 = q[7];
     const float x0[3] = {q0.x, q0.y, q0.z}, u[3] = {q2.x, q2.y, q2.z};
     float gp[3];
     int base[3];
@@ -138,10 +138,27 @@ __device__ __forceinline__ void p2g_scatter(const P2GParticle &P, float4 *tile, 
     }
 }
 
-__global__ void __launch_bounds__(kP2GWarps * 32, 4) p2g_kernel(const MpmScene *__restrict__ scenes,
+__device__ __forceinline__ void p2g_cp_async16(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+// queue the record copies of window w of the batch (lane = entry)
+__device__ __forceinline__ void p2g_prefetch(P2GWarpSmem &sm, const PState &st, int w, int nv, int lane) {
+    const int k = w * 32 + lane;
+    if (k < nv) {
+        const float4 *src = st.rec + (int64_t)sm.perm[k] * kRecQuads;
+#pragma unroll
+        for (int q = 0; q < kP2GQuads; ++q) p2g_cp_async16(&sm.rec[q][lane], src + q);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kP2GWarps * 32, 5) p2g_kernel(const MpmScene *__restrict__ scenes,
                                                                 PState st, Ws ws, float dt,
                                                                 int *status) {
-    __shared__ P2GWarpSmem smem[kP2GWarps];
+    extern __shared__ __align__(16) unsigned char p2g_smem_raw[];
+    P2GWarpSmem *smem = reinterpret_cast<P2GWarpSmem *>(p2g_smem_raw);
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -167,23 +184,33 @@ __global__ void __launch_bounds__(kP2GWarps * 32, 4) p2g_kernel(const MpmScene *
             while (r < maxcnt && nv <= kPassCap - 64) {
                 const bool a = c0 > r, b = c1 > r;
                 const unsigned ma = __ballot_sync(full, a), mb = __ballot_sync(full, b);
-                if (a) sm.perm[nv + __popc(ma & lt)] = s0 + r;
-                if (b) sm.perm[nv + __popc(ma) + __popc(mb & lt)] = s1 + r;
+                // sorted positions come from the block's cell ranges (< n); store their slots
+                if (a) sm.perm[nv + __popc(ma & lt)] = ws.order[s0 + r];
+                if (b) sm.perm[nv + __popc(ma) + __popc(mb & lt)] = ws.order[s1 + r];
                 nv += __popc(ma) + __popc(mb);
                 ++r;
             }
             __syncwarp();
-            for (int w0 = 0; w0 < nv; w0 += 32) {
-                const int k = w0 + lane;
+            // windows of 32 entries; once window w is in registers, the records
+            // of window w + 1 stream into the shared buffer while w is scattered
+            const int nwin = (nv + 31) >> 5;
+            if (nwin > 0) p2g_prefetch(sm, st, 0, nv, lane);
+            for (int w = 0; w < nwin; ++w) {
+                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+                __syncwarp();
+                const int k = w * 32 + lane;
                 bool act = k < nv;
+                float4 q[kP2GQuads];
+                if (act) {
+#pragma unroll
+                    for (int qq = 0; qq < kP2GQuads; ++qq) q[qq] = sm.rec[qq][lane];
+                }
+                __syncwarp();
+                if (w + 1 < nwin) p2g_prefetch(sm, st, w + 1, nv, lane);
                 P2GParticle P;
                 if (act) {
-                    const int idx = sm.perm[k];
-                    act = idx < ws.n;
-                    if (act) {
-                        act = p2g_load(S, st, ws.order[idx], bx, by, bz, dt, P);
-                        if (!act) atomicOr(status, MPM_ST_INTERNAL);
-                    }
+                    act = p2g_load(S, q, bx, by, bz, dt, P);
+                    if (!act) atomicOr(status, MPM_ST_INTERNAL);
                 }
                 const int cell = act ? (P.lx * 4 + P.ly) * 4 + P.lz : -1 - lane;
                 const unsigned peers = __match_any_sync(full, cell);
@@ -196,7 +223,7 @@ __global__ void __launch_bounds__(kP2GWarps * 32, 4) p2g_kernel(const MpmScene *
                     __syncwarp();
                 }
             }
-            __syncwarp();
+            __syncwarp();  // perm and the record buffers are refilled by the next batch
         }
         // flush the tile: one float4 atomic per non-zero node
         const int nb = S.n_blocks_axis;
@@ -560,17 +587,28 @@ static int persistent_grid(const Ctx &cx, int per_sm) {
 }
 
 cudaError_t launch_p2g(const Ctx &cx, float dt) {
-    // persistent: four CTAs (16 warps) per SM, never more warps than blocks
+    // more than the 48 KB of static shared memory: opt in once per device
+    static bool attr_set[64] = {false};
+    const int bytes = (int)(sizeof(P2GWarpSmem) * kP2GWarps);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
+        e = cudaFuncSetAttribute(p2g_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        if (dev >= 0 && dev < 64) attr_set[dev] = true;
+    }
+    // persistent: five CTAs (20 warps) per SM, never more warps than blocks
     int64_t want = (cx.total_blocks + kP2GWarps - 1) / kP2GWarps;
-    int grid = (int)(want < (int64_t)cx.num_sms * 4 ? want : (int64_t)cx.num_sms * 4);
+    int grid = (int)(want < (int64_t)cx.num_sms * 5 ? want : (int64_t)cx.num_sms * 5);
     if (grid < 1) grid = 1;
-    p2g_kernel<<<grid, kP2GWarps * 32, 0, cx.stream>>>(cx.scenes, cx.st, cx.ws, dt, cx.status);
+    p2g_kernel<<<grid, kP2GWarps * 32, bytes, cx.stream>>>(cx.scenes, cx.st, cx.ws, dt, cx.status);
     return cudaGetLastError();
 }
 
 cudaError_t launch_grid(const Ctx &cx, float time, float dt) {
     int64_t want = (cx.total_blocks + 3) / 4;
-    int grid = (int)(want < (int64_t)cx.num_sms * 8 ? want : (int64_t)cx.num_sms * 8);
+    int grid = (int)(want < (int64_t)cx.num_sms * 5 ? want : (int64_t)cx.num_sms * 5);
     if (grid < 1) grid = 1;
     grid_kernel<<<grid, 256, 0, cx.stream>>>(cx.scenes, cx.n_scenes, cx.ws, time, dt);
     return cudaGetLastError();
