@@ -608,7 +608,7 @@ cudaError_t launch_p2g(const Ctx &cx, float dt) {
 
 cudaError_t launch_grid(const Ctx &cx, float time, float dt) {
     int64_t want = (cx.total_blocks + 3) / 4;
-    int grid = (int)(want < (int64_t)cx.num_sms * 5 ? want : (int64_t)cx.num_sms * 5);
+    int grid = (int)(want < (int64_t)cx.num_sms * 8 ? want : (int64_t)cx.num_sms * 8);
     if (grid < 1) grid = 1;
     grid_kernel<<<grid, 256, 0, cx.stream>>>(cx.scenes, cx.n_scenes, cx.ws, time, dt);
     return cudaGetLastError();
