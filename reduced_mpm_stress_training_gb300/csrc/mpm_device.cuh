@@ -315,6 +315,202 @@ __device__ __forceinline__ void udwt(const float U[9], const float d[3], const f
                              U[r * 3 + 2] * d[2] * W[c * 3 + 2];
 }
 
+// symmetric 3x3 stored as (xx, xy, xz, yy, yz, zz)
+__device__ __forceinline__ float sym_norm(const float S[6]) {
+    return sqrtf(S[0] * S[0] + S[3] * S[3] + S[5] * S[5] + 2.0f * (S[1] * S[1] + S[2] * S[2] + S[4] * S[4]));
+}
+__device__ __forceinline__ void sym_full(const float S[6], float M[9]) {
+    M[0] = S[0]; M[1] = S[1]; M[2] = S[2];
+    M[3] = S[1]; M[4] = S[3]; M[5] = S[4];
+    M[6] = S[2]; M[7] = S[4]; M[8] = S[5];
+}
+
+// B = F F^T - I through G = F - I (B = G + G^T + G G^T), so that small strains keep their digits
+__device__ __forceinline__ void left_strain(const float F[9], float B[6]) {
+    float G[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) G[k] = F[k] - ((k % 4 == 0) ? 1.0f : 0.0f);
+    auto bij = [&](int i, int j) {
+        return G[i * 3 + j] + G[j * 3 + i] + G[i * 3] * G[j * 3] + G[i * 3 + 1] * G[j * 3 + 1] +
+               G[i * 3 + 2] * G[j * 3 + 2];
+    };
+    B[0] = bij(0, 0); B[1] = bij(0, 1); B[2] = bij(0, 2);
+    B[3] = bij(1, 1); B[4] = bij(1, 2); B[5] = bij(2, 2);
+}
+
+// Eigenvalues of a symmetric 3x3 (largest first) by the closed-form
+// trigonometric solution of the characteristic cubic (O. K. Smith,
+// "Eigenvalues of a symmetric 3x3 matrix", CACM 4(4), 1961).
+__device__ __forceinline__ void sym_eig3(const float B[6], float ev[3]) {
+    const float q = (B[0] + B[3] + B[5]) * (1.0f / 3.0f);
+    const float d0 = B[0] - q, d1 = B[3] - q, d2 = B[5] - q;
+    const float p1 = B[1] * B[1] + B[2] * B[2] + B[4] * B[4];
+    const float p2 = d0 * d0 + d1 * d1 + d2 * d2 + 2.0f * p1;
+    if (!(p2 > 0.0f)) {
+        ev[0] = ev[1] = ev[2] = q;
+        return;
+    }
+    const float p = sqrtf(p2 * (1.0f / 6.0f));
+    const float ip = 1.0f / p;
+    const float c0 = d0 * ip, c1 = B[1] * ip, c2 = B[2] * ip, c3 = d1 * ip, c4 = B[4] * ip, c5 = d2 * ip;
+    const float det = c0 * (c3 * c5 - c4 * c4) - c1 * (c1 * c5 - c4 * c2) + c2 * (c1 * c4 - c3 * c2);
+    const float r = fminf(fmaxf(0.5f * det, -1.0f), 1.0f);
+    const float a = acosf(r) * (1.0f / 3.0f);
+    ev[0] = q + 2.0f * p * cosf(a);
+    ev[2] = q + 2.0f * p * cosf(a + 2.0943951023931953f);
+    ev[1] = 3.0f * q - ev[0] - ev[2];
+}
+
+__device__ __forceinline__ void mat_mul(const float A[9], const float B[9], float C[9]) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            C[r * 3 + c] = A[r * 3] * B[c] + A[r * 3 + 1] * B[3 + c] + A[r * 3 + 2] * B[6 + c];
+}
+
+// ---------------------------------------------------------------------------
+// Sand return map + stress without an SVD.  Everything sand_return_mapping and
+// kirchoff_stress_drucker_prager (engine_stress/mpm_utils.py:87-112, :45-52)
+// compute is an isotropic function of the left Cauchy-Green tensor
+// b = F F^T = I + B: the log strains are e_i = log s_i = log(1 + beta_i) / 2
+// with beta_i the eigenvalues of B, and
+//   elastic  F = F_trial,             tau = 2 mu E + lam tr(E) I,    E = e(B)
+//   cone     F = exp(-r dev E) F_trial, tau = 2 mu E' + lam tr(E) I, E' = E - r dev E
+//   apex     F = b^{-1/2} F_trial (the polar rotation U V^T), tau = 0
+// (r = dgamma / |dev e|).  Each matrix function f(B) is evaluated in Newton
+// form on the eigenvalues a, b, c (closed form, sym_eig3):
+//   f(B) = f(a) I + f[a,b] (B - aI) + f[a,b,c] (B - aI)(B - bI),
+// with the most isolated eigenvalue first, so that the divided differences
+// divide by the large gaps only and the first-order ones of a close pair are
+// taken in closed form (log1p / expm1 / square-root identities): the result
+// stays accurate as eigenvalues coincide (F ~ I, the common case), where the
+// Jacobi SVD path is limited by its rotation angles.  Returns false (caller
+// takes the SVD path) for inverted or extremely compressed elements.
+// ---------------------------------------------------------------------------
+// log(x / y) / (x - y) for x, y > 0, finite as x -> y
+__device__ __forceinline__ float log_ratio_div(float x, float y) {
+    const float d = x - y;
+    const float u = d / y;
+    if (fabsf(u) < 1e-3f) return (1.0f - u * (0.5f - u * (1.0f / 3.0f))) / y;
+    return log1pf(u) / d;
+}
+// expm1(z) / z, finite at 0
+__device__ __forceinline__ float expm1_div(float z) {
+    if (fabsf(z) < 1e-4f) return 1.0f + z * (0.5f + z * (1.0f / 6.0f));
+    return expm1f(z) / z;
+}
+
+struct Newton3 {
+    float a, b, c;  // nodes: isolated eigenvalue first
+    float M1[6];    // B - aI
+    float M2[6];    // (B - aI)(B - bI)
+    bool iso0;      // nodes are (ev0, ev1, ev2) (else (ev2, ev1, ev0))
+};
+
+__device__ __forceinline__ void newton3_setup(const float B[6], const float ev[3], Newton3 &N) {
+    N.iso0 = (ev[0] - ev[1]) >= (ev[1] - ev[2]);
+    N.a = N.iso0 ? ev[0] : ev[2];
+    N.b = ev[1];
+    N.c = N.iso0 ? ev[2] : ev[0];
+    // B^2 (symmetric)
+    const float B2[6] = {B[0] * B[0] + B[1] * B[1] + B[2] * B[2], B[0] * B[1] + B[1] * B[3] + B[2] * B[4],
+                         B[0] * B[2] + B[1] * B[4] + B[2] * B[5], B[1] * B[1] + B[3] * B[3] + B[4] * B[4],
+                         B[1] * B[2] + B[3] * B[4] + B[4] * B[5], B[2] * B[2] + B[4] * B[4] + B[5] * B[5]};
+    const float s = N.a + N.b, p = N.a * N.b;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float id = (k == 0 || k == 3 || k == 5) ? 1.0f : 0.0f;
+        N.M1[k] = B[k] - N.a * id;
+        N.M2[k] = B2[k] - s * B[k] + p * id;
+    }
+}
+
+// f(B) from f at the sorted eigenvalues (f0 >= ...) and the first divided
+// differences of the sorted pairs d01 = f[ev0, ev1], d12 = f[ev1, ev2]
+__device__ __forceinline__ void newton3_eval(const Newton3 &N, float f0, float f2, float d01, float d12,
+                                             float out[6]) {
+    const float fa = N.iso0 ? f0 : f2;
+    const float dab = N.iso0 ? d01 : d12;
+    const float dbc = N.iso0 ? d12 : d01;
+    const float den = N.c - N.a;
+    const float d2 = den != 0.0f ? (dbc - dab) / den : 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float id = (k == 0 || k == 3 || k == 5) ? 1.0f : 0.0f;
+        out[k] = fa * id + dab * N.M1[k] + d2 * N.M2[k];
+    }
+}
+
+__device__ __forceinline__ void sym_times(const float S[6], const float A[9], float out[9]) {
+    float Sf[9];
+    sym_full(S, Sf);
+    mat_mul(Sf, A, out);
+}
+
+__device__ __forceinline__ bool sand_return_map_spectral(const MpmScene &S, const float Ft[9], float Fo[9],
+                                                         float tau[9]) {
+    const float J = Ft[0] * (Ft[4] * Ft[8] - Ft[5] * Ft[7]) - Ft[1] * (Ft[3] * Ft[8] - Ft[5] * Ft[6]) +
+                    Ft[2] * (Ft[3] * Ft[7] - Ft[4] * Ft[6]);
+    if (!(J > 0.0f)) return false;
+    float B[6], ev[3];
+    left_strain(Ft, B);
+    sym_eig3(B, ev);
+    if (!(ev[2] > -0.99f)) return false;  // smallest singular value below 0.1
+    const float mu = S.mu, lam = S.lam;
+    const float e0 = 0.5f * log1pf(ev[0]), e1 = 0.5f * log1pf(ev[1]), e2 = 0.5f * log1pf(ev[2]);
+    const float tr = e0 + e1 + e2;
+    const float h0 = e0 - tr / 3.0f, h1 = e1 - tr / 3.0f, h2 = e2 - tr / 3.0f;
+    const float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2);
+    const float dg = hn + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * S.alpha;
+    Newton3 N;
+    newton3_setup(B, ev, N);
+    const float q0 = 1.0f + ev[0], q1 = 1.0f + ev[1], q2 = 1.0f + ev[2];
+    if (dg > 0.0f && tr > 0.0f) {
+        // apex: F = b^{-1/2} F_trial, s(beta) = (1 + beta)^{-1/2},
+        // s[x, y] = -s(x) s(y) / (sqrt(1 + x) + sqrt(1 + y))
+        const float s0 = rsqrtf(q0), s1 = rsqrtf(q1), s2 = rsqrtf(q2);
+        const float d01 = -s0 * s1 / (q0 * s0 + q1 * s1);
+        const float d12 = -s1 * s2 / (q1 * s1 + q2 * s2);
+        float Sm[6];
+        newton3_eval(N, s0, s2, d01, d12, Sm);
+        sym_times(Sm, Ft, Fo);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) tau[k] = 0.0f;
+        return true;
+    }
+    // E = e(B), e(beta) = log(1 + beta) / 2
+    const float l01 = 0.5f * log_ratio_div(q0, q1), l12 = 0.5f * log_ratio_div(q1, q2);
+    float E[6];
+    newton3_eval(N, e0, e2, l01, l12, E);
+    float T[6];
+    if (dg <= 0.0f) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fo[k] = Ft[k];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) T[k] = 2.0f * mu * E[k] + ((k == 0 || k == 3 || k == 5) ? lam * tr : 0.0f);
+    } else {
+        // cone: E' = E - r (E - tr/3 I); F = exp(-r (E - tr/3 I)) F_trial,
+        // g(beta) = exp(-r (e(beta) - tr/3)), g[x, y] = g(y) expm1(-r (e(x) - e(y))) / (x - y)
+        const float r = dg / hn;
+        const float g0 = expf(-r * h0), g1 = expf(-r * h1), g2 = expf(-r * h2);
+        const float z01 = -r * l01, z12 = -r * l12;  // (e(x) - e(y)) = l (x - y)
+        const float dg01 = g1 * z01 * expm1_div(z01 * (ev[0] - ev[1]));
+        const float dg12 = g2 * z12 * expm1_div(z12 * (ev[1] - ev[2]));
+        float Gm[6];
+        newton3_eval(N, g0, g2, dg01, dg12, Gm);
+        sym_times(Gm, Ft, Fo);
+        const float k1 = 1.0f - r, k0 = r * tr / 3.0f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float id = (k == 0 || k == 3 || k == 5) ? 1.0f : 0.0f;
+            T[k] = 2.0f * mu * (k1 * E[k] + k0 * id) + lam * tr * id;
+        }
+    }
+    sym_full(T, tau);
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // Return mapping + Kirchhoff stress for one particle, fused on ONE SVD.
 // The reference (g2p_apic_and_stress, engine_stress/mpm_utils.py:284-306)
@@ -326,6 +522,7 @@ __device__ __forceinline__ void udwt(const float U[9], const float d[3], const f
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void return_map_stress(const MpmScene &S, const float Ft[9], float &yld,
                                                   float Fo[9], float tau[9]) {
+    if (S.material == MPM_SAND && sand_return_map_spectral(S, Ft, Fo, tau)) return;
     Svd d;
     svd3(Ft, d);
     const float mu = S.mu, lam = S.lam;

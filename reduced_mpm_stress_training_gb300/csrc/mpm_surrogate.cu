@@ -34,29 +34,6 @@ enum {
     kCodes = 7
 };
 
-// symmetric 3x3 stored as (xx, xy, xz, yy, yz, zz)
-__device__ __forceinline__ float sym_norm(const float S[6]) {
-    return sqrtf(S[0] * S[0] + S[3] * S[3] + S[5] * S[5] + 2.0f * (S[1] * S[1] + S[2] * S[2] + S[4] * S[4]));
-}
-__device__ __forceinline__ void sym_full(const float S[6], float M[9]) {
-    M[0] = S[0]; M[1] = S[1]; M[2] = S[2];
-    M[3] = S[1]; M[4] = S[3]; M[5] = S[4];
-    M[6] = S[2]; M[7] = S[4]; M[8] = S[5];
-}
-
-// B = F F^T - I through G = F - I (B = G + G^T + G G^T), so that small strains keep their digits
-__device__ __forceinline__ void left_strain(const float F[9], float B[6]) {
-    float G[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) G[k] = F[k] - ((k % 4 == 0) ? 1.0f : 0.0f);
-    auto bij = [&](int i, int j) {
-        return G[i * 3 + j] + G[j * 3 + i] + G[i * 3] * G[j * 3] + G[i * 3 + 1] * G[j * 3 + 1] +
-               G[i * 3 + 2] * G[j * 3 + 2];
-    };
-    B[0] = bij(0, 0); B[1] = bij(0, 1); B[2] = bij(0, 2);
-    B[3] = bij(1, 1); B[4] = bij(1, 2); B[5] = bij(2, 2);
-}
-
 // Poisson's ratio and friction angle (degrees) of a scene from lam, mu and
 // alpha = sqrt(2/3) 2 sin(phi) / (3 - sin(phi)) (engine_stress/mpm_solver_warp.py:116)
 __device__ __forceinline__ void scene_nu_phi(const MpmScene &S, float &nu, float &phi_deg) {
@@ -73,37 +50,6 @@ __device__ __forceinline__ void features(const float B[6], float rho, float nu, 
     x[9] = (log10f(fmaxf(rho, 1e-30f)) + 2.5f) * (1.0f / 1.5f);
     x[10] = (nu - 0.3f) * 10.0f;
     x[11] = (phi - 30.0f) * 0.1f;
-}
-
-// Eigenvalues of a symmetric 3x3 (largest first) by the closed-form
-// trigonometric solution of the characteristic cubic (O. K. Smith,
-// "Eigenvalues of a symmetric 3x3 matrix", CACM 4(4), 1961).
-__device__ __forceinline__ void sym_eig3(const float B[6], float ev[3]) {
-    const float q = (B[0] + B[3] + B[5]) * (1.0f / 3.0f);
-    const float d0 = B[0] - q, d1 = B[3] - q, d2 = B[5] - q;
-    const float p1 = B[1] * B[1] + B[2] * B[2] + B[4] * B[4];
-    const float p2 = d0 * d0 + d1 * d1 + d2 * d2 + 2.0f * p1;
-    if (!(p2 > 0.0f)) {
-        ev[0] = ev[1] = ev[2] = q;
-        return;
-    }
-    const float p = sqrtf(p2 * (1.0f / 6.0f));
-    const float ip = 1.0f / p;
-    const float c0 = d0 * ip, c1 = B[1] * ip, c2 = B[2] * ip, c3 = d1 * ip, c4 = B[4] * ip, c5 = d2 * ip;
-    const float det = c0 * (c3 * c5 - c4 * c4) - c1 * (c1 * c5 - c4 * c2) + c2 * (c1 * c4 - c3 * c2);
-    const float r = fminf(fmaxf(0.5f * det, -1.0f), 1.0f);
-    const float a = acosf(r) * (1.0f / 3.0f);
-    ev[0] = q + 2.0f * p * cosf(a);
-    ev[2] = q + 2.0f * p * cosf(a + 2.0943951023931953f);
-    ev[1] = 3.0f * q - ev[0] - ev[2];
-}
-
-__device__ __forceinline__ void mat_mul(const float A[9], const float B[9], float C[9]) {
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-            C[r * 3 + c] = A[r * 3] * B[c] + A[r * 3 + 1] * B[3 + c] + A[r * 3 + 2] * B[6 + c];
 }
 
 // exp(X) for symmetric X with |X| <= 0.25: Taylor series to degree 6 in
