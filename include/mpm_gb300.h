@@ -244,6 +244,12 @@ int64_t mpm_mlp_param_bytes(void);
  * the summed squared error to *loss (device float).  y may be NULL. */
 int mpm_mlp_forward(const void *params, const float *x, float *y, const float *target, void *zsave,
                     void *dy, float *loss, float grad_scale, int64_t n, void *stream);
+/* The same forward on the tcgen05 tensor cores (accumulators in tensor
+ * memory, one 128-row tile per CTA step).  err: one device int32 the
+ * kernel ORs 1 into if a tensor-core completion wait ran out (results then
+ * incomplete); the caller zeroes it. */
+int mpm_mlp_forward_tc(const void *params, const float *x, float *y, const float *target, void *zsave,
+                       void *dy, float *loss, float grad_scale, int64_t n, int32_t *err, void *stream);
 /* Adds the parameter gradient of the forward's loss into grad (fp32,
  * MPM_MLP_PARAMS).  work: 2*n*128 bf16 scratch. */
 int mpm_mlp_backward(const void *params, const float *x, const void *zsave, const void *dy, void *work,

@@ -97,6 +97,8 @@ _SIGS = {
     "mpm_mlp_param_bytes": ([], C.c_int64),
     "mpm_mlp_forward": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p, C.c_float, C.c_int64, C.c_void_p], C.c_int),
+    "mpm_mlp_forward_tc": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                            C.c_void_p, C.c_float, C.c_int64, C.c_void_p, C.c_void_p], C.c_int),
     "mpm_mlp_backward": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                           C.c_int64, C.c_void_p], C.c_int),
     "mpm_mlp_adam": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,

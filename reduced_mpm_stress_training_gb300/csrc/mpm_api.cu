@@ -303,6 +303,16 @@ int mpm_surrogate_features(const MpmScene *scene, const float *F, const float *s
     return MPM_OK;
 }
 
+int mpm_mlp_forward_tc(const void *params, const float *x, float *y, const float *target, void *zsave, void *dy,
+                       float *loss, float grad_scale, int64_t n, int32_t *err, void *stream) {
+    if (!params || !err || n < 0 || (n > 0 && !x)) return MPM_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(params) & 15) return MPM_ERR_ARG;
+    if ((target != nullptr) != (dy != nullptr)) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_mlp_forward_tc(params, x, y, target, zsave, dy, loss, grad_scale, n, err, num_sms(),
+                                         static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
 int mpm_surrogate_apply(const MpmScene *scene, const void *mlp_params, const MpmSurrogateConfig *cfg,
                         const float *F_trial, float *F, float *stress, int32_t *codes, int64_t n, void *stream) {
     if (!scene || !mlp_params || !surrogate_cfg_ok(cfg) || n < 0) return MPM_ERR_ARG;

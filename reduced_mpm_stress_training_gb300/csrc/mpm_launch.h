@@ -49,6 +49,11 @@ int64_t substep_grid_bytes(int64_t total_blocks, int64_t n);
 cudaError_t launch_save_grid(const Ctx &cx, void *dst);
 cudaError_t launch_load_grid(const Ctx &cx, const void *src);
 cudaError_t launch_clear_grid(const Ctx &cx);
+// tensor-core (tcgen05) network forward (mpm_mlp_tc.cu)
+int64_t mlp_tc_smem_bytes();
+cudaError_t launch_mlp_forward_tc(const void *params, const float *x, float *y, const float *target, void *zsave,
+                                  void *dy, float *loss, float grad_scale, int64_t n, int *err, int num_sms,
+                                  cudaStream_t stream);
 cudaError_t launch_features(const MpmScene &scene, const float *F, const float *stress, float *x, float *y,
                             int64_t n, cudaStream_t stream);
 

@@ -81,3 +81,27 @@ def test_training_lowers_the_loss(cuda):
         last = net.train_step(xt, tt)
     last = last.item()
     assert last < 0.1 * first, (first, last)
+
+
+@pytest.mark.parametrize("n", [1, 127, 128, 1000, 70000])
+def test_tcgen05_forward_matches_oracle(cuda, n):
+    """The tcgen05 / tensor-memory forward: same outputs as the oracle (and as
+    the mma.sync forward) at the same bf16 rounding points."""
+    x, t = _data(n, 7 + n)
+    net = StressMLP(cuda, seed=3)
+    xt = torch.from_numpy(x).to(cuda)
+    err = torch.zeros(1, dtype=torch.int32, device=cuda)
+    y = torch.full((n, M.OUT), float("nan"), device=cuda)
+    A_ = net.lib
+    from reduced_mpm_stress_training_gb300 import _capi as CAPI
+    CAPI.check(A_.mpm_mlp_forward_tc(net.params.data_ptr(), xt.data_ptr(), y.data_ptr(), None, None, None, None,
+                                     0.0, n, err.data_ptr(), torch.cuda.current_stream().cuda_stream),
+               "mpm_mlp_forward_tc")
+    torch.cuda.synchronize()
+    assert err.item() == 0
+    ref = M.forward(net.master.cpu().numpy(), x)["y"]
+    yg = y.cpu().numpy()
+    assert np.isfinite(yg).all()
+    assert rel(yg, ref) < 2e-3, rel(yg, ref)
+    y2 = net.forward(xt).cpu().numpy()
+    assert rel(yg, y2) < 2e-3
