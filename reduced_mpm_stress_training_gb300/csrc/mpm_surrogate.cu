@@ -16,6 +16,7 @@
 // deviatoric direction (the reference's U diag(exp(e - dgamma h/|h|)) V^T
 // rewritten in the spatial frame).
 #include "mpm_mlp.cuh"
+#include "mpm_mlp_tc.cuh"
 #include "mpm_launch.h"
 
 namespace mpm {
@@ -342,64 +343,6 @@ __device__ __forceinline__ void count_codes(int cnt[kCodes], int *stats) {
     }
 }
 
-__global__ void __launch_bounds__(kSurWarps * 32, 1)
-    surrogate_kernel(const MpmScene *__restrict__ scenes, PState st, Ws ws, const __nv_bfloat16 *__restrict__ wts,
-                     const float *__restrict__ bias, MpmSurrogateConfig cfg, int2 *__restrict__ fallback,
-                     int *__restrict__ stats, int *__restrict__ status) {
-    extern __shared__ __align__(16) unsigned char sur_smem_raw[];
-    SurSmem &sm = *reinterpret_cast<SurSmem *>(sur_smem_raw);
-    load_weights(sm.w, wts, bias);
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    SurWarp &sw = sm.warp[warp];
-    const int wpc = ws.chunk_size / 32;  // warps per chunk
-    const int n_items = *ws.n_chunks * wpc;
-    int cnt[kCodes];
-#pragma unroll
-    for (int k = 0; k < kCodes; ++k) cnt[k] = 0;
-    for (int item = blockIdx.x * kSurWarps + warp; item < n_items; item += gridDim.x * kSurWarps) {
-        const int4 ch = ws.chunks[item / wpc];
-        const int sub = item % wpc;
-        const int count = min(ch.z - sub * 32, 32);
-        if (ch.w < 0 || count <= 0) continue;  // warp-uniform
-        const MpmScene &S = scenes[ch.w];
-        const int pos = ch.y + sub * 32 + lane;
-        const bool valid = lane < count && pos < ws.n;
-        float F[9], Fo[9], tau[9];
-        if (valid) {
-            ld_F(st, pos, F);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 9; ++k) F[k] = (k % 4 == 0) ? 1.0f : 0.0f;
-        }
-        int code = FB_MATERIAL;
-        if (S.material == MPM_SAND)  // warp-uniform: one scene per chunk
-            code = surrogate_warp(sm.w, sw, S, cfg, F, valid, Fo, tau);
-        const bool accepted = valid && (code == ACC_ELASTIC || code == ACC_PLASTIC);
-        if (accepted) {
-            float chk = 0.0f;
-#pragma unroll
-            for (int k = 0; k < 9; ++k) chk += fabsf(Fo[k]) + fabsf(tau[k]);
-            if (!isfinite(chk)) atomicOr(status, MPM_ST_NONFINITE);
-            st_F_tau(st, pos, Fo, tau);
-        }
-        // fallback list: one atomic per warp
-        const bool fb = valid && !accepted;
-        const unsigned m = __ballot_sync(0xffffffffu, fb);
-        if (m) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(stats + MPM_SUR_LAST_FALLBACKS, __popc(m));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (fb) fallback[base + __popc(m & ((1u << lane) - 1u))] = make_int2(pos, ch.w);
-        }
-        if (valid) {
-#pragma unroll
-            for (int k = 0; k < kCodes; ++k) cnt[k] += (code == k);
-        }
-    }
-    count_codes(cnt, stats);
-}
-
 // The surrogate on plain arrays of one scene: F_trial (n,9) -> F (n,9),
 // stress (n,9), outcome code (n); gated-out rows take the SVD return map.
 __global__ void __launch_bounds__(kSurWarps * 32, 1)
@@ -436,6 +379,92 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
     }
 }
 
+// The in-step stage on the tcgen05 tensor cores: one CTA of 128 threads walks
+// the G2P chunk list in tiles of up to 128 particles of one scene (thread =
+// particle), runs the exact pre-pass, and -- if any particle of the tile
+// needs it -- the network on the tile (mpm_mlp_tc.cuh), then the correction
+// and gate.  A timed-out tensor-core wait raises MPM_ST_INTERNAL.
+constexpr int kTcRows = mlptc::kRows;
+
+__global__ void __launch_bounds__(kTcRows, 2)
+    surrogate_tc_kernel(const MpmScene *__restrict__ scenes, PState st, Ws ws, const __nv_bfloat16 *__restrict__ wts,
+                        const float *__restrict__ bias, MpmSurrogateConfig cfg, int2 *__restrict__ fallback,
+                        int *__restrict__ stats, int *__restrict__ status) {
+    extern __shared__ __align__(128) unsigned char tc_raw[];
+    mlptc::TcSmem &s = *reinterpret_cast<mlptc::TcSmem *>(tc_raw);
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t tbase = mlptc::tc_setup(s, wts, bias);
+    uint32_t phase = 0;
+    bool ok = true;
+    const int tpc = (ws.chunk_size + kTcRows - 1) / kTcRows;  // tiles per chunk
+    const int n_items = *ws.n_chunks * tpc;
+    int cnt[kCodes];
+#pragma unroll
+    for (int k = 0; k < kCodes; ++k) cnt[k] = 0;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+        const int4 ch = ws.chunks[item / tpc];
+        const int sub = item % tpc;
+        const int count = min(ch.z - sub * kTcRows, kTcRows);
+        if (ch.w < 0 || count <= 0) continue;  // CTA-uniform
+        const MpmScene &S = scenes[ch.w];
+        const int pos = ch.y + sub * kTcRows + tid;
+        const bool valid = tid < count && pos < ws.n;
+        float F[9], Fo[9], tau[9];
+        if (valid) {
+            ld_F(st, pos, F);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) F[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+        }
+        int code = FB_MATERIAL;
+        if (S.material == MPM_SAND) {  // CTA-uniform: one scene per chunk
+            float B[6];
+            left_strain(F, B);
+            const float rho = sym_norm(B);
+            Pre p;
+            pre_particle(S, cfg, B, rho, p);
+            code = valid ? p.code : FB_DOMAIN;
+            const bool need = code == ACC_ELASTIC || code == ACC_PLASTIC;
+            if (__syncthreads_or(need ? 1 : 0)) {
+                float xi[12], nu, phi;
+                scene_nu_phi(S, nu, phi);
+                features(B, rho, nu, phi, xi);
+                mlptc::tc_store_inputs(s, xi);
+                float out[16];
+                ok = mlptc::tc_tile_forward(s, tbase, phase, out, nullptr);
+                if (!ok) break;
+                if (need) {
+                    const float y6[6] = {out[0], out[1], out[2], out[3], out[4], out[5]};
+                    code = post_particle(S, cfg, F, B, rho, p, y6, Fo, tau);
+                }
+            }
+        }
+        const bool accepted = valid && (code == ACC_ELASTIC || code == ACC_PLASTIC);
+        if (accepted) {
+            float chk = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) chk += fabsf(Fo[k]) + fabsf(tau[k]);
+            if (!isfinite(chk)) atomicOr(status, MPM_ST_NONFINITE);
+            st_F_tau(st, pos, Fo, tau);
+        }
+        const bool fb = valid && !accepted;
+        const unsigned m = __ballot_sync(0xffffffffu, fb);
+        if (m) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(stats + MPM_SUR_LAST_FALLBACKS, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (fb) fallback[base + __popc(m & ((1u << lane) - 1u))] = make_int2(pos, ch.w);
+        }
+        if (valid) {
+#pragma unroll
+            for (int k = 0; k < kCodes; ++k) cnt[k] += (code == k);
+        }
+    }
+    if (!ok && tid == 0) atomicOr(status, MPM_ST_INTERNAL);
+    count_codes(cnt, stats);
+    mlptc::tc_teardown(s, tbase, ok, phase);
+}
+
 // SVD return map for the listed particles (the exact path)
 __global__ void fallback_kernel(const MpmScene *__restrict__ scenes, PState st, const int2 *__restrict__ list,
                                 const int *__restrict__ stats, int *__restrict__ status) {
@@ -467,7 +496,8 @@ static cudaError_t surrogate_attrs() {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64 || !attr_set[dev]) {
-        e = cudaFuncSetAttribute(sur::surrogate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        e = cudaFuncSetAttribute(sur::surrogate_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(mlptc::TcSmem));
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(sur::surrogate_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      bytes);
@@ -480,7 +510,7 @@ static cudaError_t surrogate_attrs() {
 cudaError_t launch_surrogate(const Ctx &cx, const void *mlp_params, const MpmSurrogateConfig &cfg,
                              int2 *fallback, int *stats) {
     using namespace sur;
-    const int bytes = (int)sizeof(SurSmem);
+    const int bytes = (int)sizeof(mlptc::TcSmem);
     cudaError_t e = surrogate_attrs();
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(stats + MPM_SUR_LAST_FALLBACKS, 0, sizeof(int), cx.stream);
@@ -489,11 +519,11 @@ cudaError_t launch_surrogate(const Ctx &cx, const void *mlp_params, const MpmSur
     const float *b = reinterpret_cast<const float *>(static_cast<const char *>(mlp_params) +
                                                      (int64_t)mlp::W_COUNT * 2);
     // records live in st2 (G2P wrote the updated, sorted records there)
-    const int64_t items = ((int64_t)cx.ws.max_chunks * (cx.ws.chunk_size / 32) + kSurWarps - 1) / kSurWarps;
-    int grid = (int)(items < cx.num_sms ? items : cx.num_sms);
+    const int64_t items = (int64_t)cx.ws.max_chunks * ((cx.ws.chunk_size + kTcRows - 1) / kTcRows);
+    int grid = (int)(items < 2 * (int64_t)cx.num_sms ? items : 2 * (int64_t)cx.num_sms);
     if (grid < 1) grid = 1;
-    surrogate_kernel<<<grid, kSurWarps * 32, bytes, cx.stream>>>(cx.scenes, cx.st2, cx.ws, w, b, cfg, fallback,
-                                                                 stats, cx.status);
+    surrogate_tc_kernel<<<grid, kTcRows, bytes, cx.stream>>>(cx.scenes, cx.st2, cx.ws, w, b, cfg, fallback, stats,
+                                                             cx.status);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     int fgrid = cx.num_sms * 4;

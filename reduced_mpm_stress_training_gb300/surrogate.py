@@ -56,8 +56,12 @@ def init_master(seed: int = 0) -> np.ndarray:
 class StressMLP:
     """The surrogate network on one device, with its Adam state."""
 
-    def __init__(self, device="cuda:0", seed: int = 0, master: np.ndarray | None = None):
+    def __init__(self, device="cuda:0", seed: int = 0, master: np.ndarray | None = None,
+                 tensor_memory: bool = True):
+        """tensor_memory: run the forward on the tcgen05 tensor cores
+        (mpm_mlp_forward_tc) instead of the mma.sync kernel."""
         self.lib = A.load()
+        self.tensor_memory = bool(tensor_memory)
         if self.lib.mpm_mlp_param_bytes() != W_COUNT * 2 + (P_COUNT - W_COUNT) * 4:
             raise ImportError("libmpm_gb300 network layout differs from the binding")
         self.device = torch.device(device)
@@ -72,6 +76,7 @@ class StressMLP:
         self.refresh()
         self.step_count = 0
         self.loss = torch.zeros(1, dtype=torch.float32, device=self.device)
+        self.tc_error = torch.zeros(1, dtype=torch.int32, device=self.device)
         self._bufs: dict = {}
 
     # -- parameters ---------------------------------------------------------
@@ -109,9 +114,23 @@ class StressMLP:
         if x.shape[1:] != (IN,) or x.dtype != torch.float32:
             raise ValueError("x must be float32 (n, 12)")
         y = out if out is not None else torch.empty(n, OUT, dtype=torch.float32, device=self.device)
-        A.check(self.lib.mpm_mlp_forward(_ptr(self.params), _ptr(x), _ptr(y), None, None, None, None,
-                                         0.0, n, _stream(self.device)), "mpm_mlp_forward")
+        self._forward(x, y, None, None, None, None, 0.0, n)
         return y
+
+    def _forward(self, x, y, target, z, dy, loss, grad_scale, n) -> None:
+        st = _stream(self.device)
+        if self.tensor_memory:
+            A.check(self.lib.mpm_mlp_forward_tc(_ptr(self.params), _ptr(x), _ptr(y), _ptr(target), _ptr(z),
+                                                _ptr(dy), _ptr(loss), grad_scale, n, _ptr(self.tc_error), st),
+                    "mpm_mlp_forward_tc")
+        else:
+            A.check(self.lib.mpm_mlp_forward(_ptr(self.params), _ptr(x), _ptr(y), _ptr(target), _ptr(z),
+                                             _ptr(dy), _ptr(loss), grad_scale, n, st), "mpm_mlp_forward")
+
+    def check_tensor_cores(self) -> None:
+        """Raise if a tensor-core completion wait of the forward ever ran out."""
+        if int(self.tc_error.item()):
+            raise RuntimeError("tcgen05 forward: a tensor-core completion wait timed out")
 
     def loss_and_grad(self, x: torch.Tensor, target: torch.Tensor, accumulate: bool = False,
                       grad_scale: float | None = None) -> torch.Tensor:
@@ -126,9 +145,7 @@ class StressMLP:
             self.grad.zero_()
         self.loss.zero_()
         st = _stream(self.device)
-        A.check(self.lib.mpm_mlp_forward(_ptr(self.params), _ptr(x), None, _ptr(target), _ptr(b["z"]),
-                                         _ptr(b["dy"]), _ptr(self.loss), grad_scale, n, st),
-                "mpm_mlp_forward")
+        self._forward(x, None, target, b["z"], b["dy"], self.loss, grad_scale, n)
         A.check(self.lib.mpm_mlp_backward(_ptr(self.params), _ptr(x), _ptr(b["z"]), _ptr(b["dy"]),
                                           _ptr(b["work"]), _ptr(self.grad), n, st), "mpm_mlp_backward")
         return self.loss / (n * OUT)
@@ -352,6 +369,7 @@ def train(net: StressMLP, x: torch.Tensor, y: torch.Tensor, steps: int, batch: i
         net.adam(cur)
         if log_every and (s % log_every == 0 or s == steps - 1):
             log.append((s, float(loss.item())))
+    net.check_tensor_cores()
     return log
 
 
