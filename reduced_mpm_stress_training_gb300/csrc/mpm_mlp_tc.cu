@@ -31,7 +31,7 @@ struct TcIO {
     int64_t n;
 };
 
-__global__ void __launch_bounds__(kRows, 1) mlp_forward_tc_kernel(const __nv_bfloat16 *__restrict__ w,
+__global__ void __launch_bounds__(kThreads, 2) mlp_forward_tc_kernel(const __nv_bfloat16 *__restrict__ w,
                                                                   const float *__restrict__ b, TcIO io,
                                                                   int *__restrict__ err) {
     extern __shared__ __align__(128) unsigned char tc_smem_raw[];
@@ -42,12 +42,15 @@ __global__ void __launch_bounds__(kRows, 1) mlp_forward_tc_kernel(const __nv_bfl
     bool ok = true;
     const int64_t tiles = (io.n + kRows - 1) / kRows;
     for (int64_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-        const int64_t row = tile * kRows + tid;
+        const int64_t row = tile * kRows + (tid & (kRows - 1));
         const bool valid = row < io.n;
-        float v[12];
+        const bool lead = tid < kRows;  // the thread that owns the row's inputs and outputs
+        if (lead) {
+            float v[12];
 #pragma unroll
-        for (int k = 0; k < 12; ++k) v[k] = valid ? io.x[row * IN + k] : 0.0f;
-        tc_store_inputs(s, v);
+            for (int k = 0; k < 12; ++k) v[k] = valid ? io.x[row * IN + k] : 0.0f;
+            tc_store_inputs(s, v);
+        }
         __nv_bfloat16 *z[3] = {nullptr, nullptr, nullptr};
         if (io.z && valid)
             for (int l = 0; l < 3; ++l) z[l] = io.z + (int64_t)l * io.n * H + row * H;
@@ -58,6 +61,7 @@ __global__ void __launch_bounds__(kRows, 1) mlp_forward_tc_kernel(const __nv_bfl
 #pragma unroll
         for (int c = 0; c < N4; ++c) {
             float d = 0.0f;
+            if (!lead) break;
             if (valid && c < OUT) {
                 if (io.y) io.y[row * OUT + c] = out[c];
                 if (io.target) {
@@ -101,8 +105,8 @@ cudaError_t launch_mlp_forward_tc(const void *params, const float *x, float *y, 
     const float *b = reinterpret_cast<const float *>(static_cast<const char *>(params) + (int64_t)mlp::W_COUNT * 2);
     TcIO io{x, y, target, static_cast<__nv_bfloat16 *>(zsave), static_cast<__nv_bfloat16 *>(dy), loss, grad_scale, n};
     const int64_t tiles = (n + kRows - 1) / kRows;
-    const int grid = (int)(tiles < num_sms ? tiles : num_sms);
-    mlp_forward_tc_kernel<<<grid, kRows, bytes, stream>>>(w, b, io, err);
+    const int grid = (int)(tiles < 2 * (int64_t)num_sms ? tiles : 2 * (int64_t)num_sms);
+    mlp_forward_tc_kernel<<<grid, kThreads, bytes, stream>>>(w, b, io, err);
     return cudaGetLastError();
 }
 

@@ -10,7 +10,8 @@ namespace mlptc {
 
 using namespace mpm::mlp;
 
-constexpr int kRows = 128;                 // tile rows = threads = TMEM lanes
+constexpr int kRows = 128;                 // tile rows = TMEM lanes
+constexpr int kThreads = 256;              // two threads per row: each takes half of the columns
 constexpr int kSlab = kRows * 16 * 2;      // bytes of one 128 x 16 bf16 K slab (4 KB)
 constexpr int kWSlab = H * 16 * 2;         // bytes of one 128(N) x 16 weight slab (4 KB)
 constexpr int kW4Slab = N4 * 16 * 2;       // 16(N) x 16 weight slab (512 B)
@@ -174,7 +175,7 @@ __device__ __forceinline__ void tc_teardown(TcSmem &s, uint32_t tbase, bool ok, 
     }
 }
 
-// Thread t's input row into the input slab: 12 features + 4 zeros.
+// Row t's inputs into the input slab (12 features + 4 zeros); threads t < 128 only.
 __device__ __forceinline__ void tc_store_inputs(TcSmem &s, const float v[12]) {
     const int t = threadIdx.x;
     *reinterpret_cast<uint4 *>(s.x + chunk_off(t, 0, kSlab)) =
@@ -183,14 +184,17 @@ __device__ __forceinline__ void tc_store_inputs(TcSmem &s, const float v[12]) {
         make_uint4(pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]), 0u, 0u);
 }
 
-// The four layers on the 128-row tile whose inputs are in s.x.  Thread t gets
-// row t's 16 (padded) outputs, bias added, in out; with z != null it also
-// writes the bf16 pre-activations of layer l to z[l] (row pointers, may be
-// null for padding rows).  Returns false (uniformly) on a timed-out wait.
+// The four layers on the 128-row tile whose inputs are in s.x.  Threads t and
+// t + 128 share row t (TMEM lanes are reachable from warps w and w + 4) and
+// take columns 0-63 and 64-127 of the hidden layers.  Thread t < 128 gets row
+// t's 16 (padded) outputs, bias added, in out; with z != null the bf16
+// pre-activations of layer l go to z[l] (row pointers, null for padding
+// rows).  Returns false (uniformly) on a timed-out wait.
 __device__ __forceinline__ bool tc_tile_forward(TcSmem &s, uint32_t tbase, uint32_t &phase, float out[16],
                                                 __nv_bfloat16 *const z[3]) {
     const int tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t tlane = tbase + ((uint32_t)(warp * 32) << 16);
+    const int row = tid & (kRows - 1), half = tid >> 7;
+    const uint32_t tlane = tbase + ((uint32_t)((warp & 3) * 32) << 16);
     for (int layer = 0; layer < 4; ++layer) {
         fence_async_smem();
         tc_before_sync();
@@ -218,10 +222,10 @@ __device__ __forceinline__ bool tc_tile_forward(TcSmem &s, uint32_t tbase, uint3
         if (layer < 3) {
             // the layer's MMAs are done reading s.h: overwrite it with the next activations
 #pragma unroll 1
-            for (int c0 = 0; c0 < H; c0 += 32) {
+            for (int c0 = half * (H / 2); c0 < (half + 1) * (H / 2); c0 += 32) {
                 float acc[32];
                 tmem_ld32(tlane + (uint32_t)c0, acc);
-                act_chunk(s, acc, s.bias + layer * H, tid, c0, z ? z[layer] : nullptr);
+                act_chunk(s, acc, s.bias + layer * H, row, c0, z ? z[layer] : nullptr);
             }
         } else {
             float acc[32];

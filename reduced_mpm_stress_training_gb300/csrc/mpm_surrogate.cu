@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(kSurWarps * 32, 1)
 // and gate.  A timed-out tensor-core wait raises MPM_ST_INTERNAL.
 constexpr int kTcRows = mlptc::kRows;
 
-__global__ void __launch_bounds__(kTcRows, 2)
+__global__ void __launch_bounds__(mlptc::kThreads, 2)
     surrogate_tc_kernel(const MpmScene *__restrict__ scenes, PState st, Ws ws, const __nv_bfloat16 *__restrict__ wts,
                         const float *__restrict__ bias, MpmSurrogateConfig cfg, int2 *__restrict__ fallback,
                         int *__restrict__ stats, int *__restrict__ status) {
@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(kTcRows, 2)
         if (ch.w < 0 || count <= 0) continue;  // CTA-uniform
         const MpmScene &S = scenes[ch.w];
         const int pos = ch.y + sub * kTcRows + tid;
-        const bool valid = tid < count && pos < ws.n;
+        const bool valid = tid < kTcRows && tid < count && pos < ws.n;  // threads >= 128 help the network only
         float F[9], Fo[9], tau[9];
         if (valid) {
             ld_F(st, pos, F);
@@ -426,10 +426,12 @@ __global__ void __launch_bounds__(kTcRows, 2)
             code = valid ? p.code : FB_DOMAIN;
             const bool need = code == ACC_ELASTIC || code == ACC_PLASTIC;
             if (__syncthreads_or(need ? 1 : 0)) {
-                float xi[12], nu, phi;
-                scene_nu_phi(S, nu, phi);
-                features(B, rho, nu, phi, xi);
-                mlptc::tc_store_inputs(s, xi);
+                if (tid < kTcRows) {
+                    float xi[12], nu, phi;
+                    scene_nu_phi(S, nu, phi);
+                    features(B, rho, nu, phi, xi);
+                    mlptc::tc_store_inputs(s, xi);
+                }
                 float out[16];
                 ok = mlptc::tc_tile_forward(s, tbase, phase, out, nullptr);
                 if (!ok) break;
@@ -522,7 +524,7 @@ cudaError_t launch_surrogate(const Ctx &cx, const void *mlp_params, const MpmSur
     const int64_t items = (int64_t)cx.ws.max_chunks * ((cx.ws.chunk_size + kTcRows - 1) / kTcRows);
     int grid = (int)(items < 2 * (int64_t)cx.num_sms ? items : 2 * (int64_t)cx.num_sms);
     if (grid < 1) grid = 1;
-    surrogate_tc_kernel<<<grid, kTcRows, bytes, cx.stream>>>(cx.scenes, cx.st2, cx.ws, w, b, cfg, fallback, stats,
+    surrogate_tc_kernel<<<grid, mlptc::kThreads, bytes, cx.stream>>>(cx.scenes, cx.st2, cx.ws, w, b, cfg, fallback, stats,
                                                              cx.status);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;

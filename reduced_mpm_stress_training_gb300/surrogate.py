@@ -383,3 +383,41 @@ def stress_errors(tau: torch.Tensor, tau_ref: torch.Tensor) -> dict:
     q = torch.quantile(row[ok][:1_000_000].float(), torch.tensor([0.5, 0.99, 1.0], device=row.device))
     return {"rel_l2": float(d.norm() / r.norm().clamp_min(1e-30)), "row_p50": float(q[0]),
             "row_p99": float(q[1]), "row_max": float(q[2])}
+
+
+def time_forward(rows: int = 1 << 20, device="cuda:0", reps: int = 20) -> dict:
+    """Milliseconds per forward of ``rows`` rows: tcgen05 kernel and mma.sync
+    kernel, CUDA events (random network, random inputs)."""
+    dev = torch.device(device)
+    g = torch.Generator(device=dev).manual_seed(0)
+    x = torch.randn(rows, IN, generator=g, device=dev)
+    out = {}
+    for name, tc in (("tcgen05", True), ("mma_sync", False)):
+        net = StressMLP(dev, seed=0, tensor_memory=tc)
+        y = torch.empty(rows, OUT, device=dev)
+        for _ in range(3):
+            net.forward(x, out=y)
+        st = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            net.forward(x, out=y)
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        if tc:
+            net.check_tensor_cores()
+        ms = e0.elapsed_time(e1) / reps
+        flops = 2.0 * rows * (IN * HID + HID * HID * 2 + HID * OUT)
+        out[name] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12}
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="time the stress-network forward kernels")
+    ap.add_argument("--rows", type=int, default=1 << 20)
+    ap.add_argument("--reps", type=int, default=20)
+    a = ap.parse_args()
+    print(json.dumps(time_forward(a.rows, reps=a.reps)))
