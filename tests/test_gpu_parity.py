@@ -282,3 +282,72 @@ def test_chunk_size_does_not_change_results(cuda, chunk):
     errs = compare(sim, ref, fields=("x", "v", "F"))
     tol = _step_tol(ref, ref64, errs)
     assert all(errs[f] < tol[f] for f in errs), (errs, tol)
+
+
+def _dev_norm_and_trace(tau):
+    """Per particle: Frobenius norm of the deviator and the trace of (n, 9) matrices."""
+    t = tau.reshape(-1, 3, 3).astype(np.float64)
+    t = 0.5 * (t + t.transpose(0, 2, 1))
+    tr = np.trace(t, axis1=1, axis2=2)
+    dev = t - tr[:, None, None] / 3.0 * np.eye(3)
+    return np.sqrt((dev * dev).sum(axis=(1, 2))), tr
+
+
+@pytest.mark.parametrize("name", ["sand_column_1m", "metal_block_1m"])
+def test_full_size_workload(cuda, name):
+    """The 1,048,576-particle, 128^3 workloads at full size and full length.
+
+    5 substeps in lockstep with the float32 oracle at the per-substep
+    tolerance, then the rest of the 1,000 substeps on the GPU alone, checked
+    through properties that hold at any size: no status bits, finite state,
+    every particle inside the domain, the returned stress inside the yield
+    surface of its material (Drucker-Prager: |dev tau| + alpha tr tau <= 0;
+    von Mises: |dev 2 mu log(sigma)| <= yield stress), and the grid mass of a
+    fresh P2G equal to the particles' total mass (partition of unity)."""
+    sc = getattr(S, name)()
+    sim = gpu_sim(sc)
+    ref = oracle_sim(sc)
+    ref64 = oracle_sim(sc, bits=64)
+    lockstep = 5
+    for k in range(lockstep):
+        sim.p2g2p(k, sc.dt)
+        ref.p2g2p(sc.dt)
+        ref64.p2g2p(sc.dt)
+    errs = compare(sim, ref, fields=("x", "v", "F"))
+    tol = _step_tol(ref, ref64, errs)
+    assert all(errs[f] < tol[f] for f in errs), (errs, tol)
+    g = gpu_state(sim)
+    ok, info = within_fp32_floor(g["stress"], ref.stress, ref64.stress)
+    assert ok, info
+    del ref, ref64
+
+    for k in range(lockstep, sc.substeps):
+        sim.p2g2p(k, sc.dt)
+    assert sim.check_status() == 0
+    g = gpu_state(sim)
+    for f in ("x", "v", "F", "stress"):
+        assert np.isfinite(g[f]).all(), f
+    assert (g["x"] > 0).all() and (g["x"] < sc.grid_lim).all()
+    assert np.abs(g["u"]).max() > 1e-3  # the material moved
+    mu = sc.E / (2 * (1 + sc.nu))
+    if sc.material == "sand":
+        alpha = float(np.sqrt(2.0 / 3.0) * 2 * np.sin(np.radians(sc.friction_angle))
+                      / (3 - np.sin(np.radians(sc.friction_angle))))
+        dn, tr = _dev_norm_and_trace(g["stress"])
+        scale = np.sqrt(dn * dn + tr * tr / 3.0)
+        assert scale.max() > 1e3  # gravity loaded the column
+        assert (dn + alpha * tr <= 1e-4 * scale + 1.0).all(), float((dn + alpha * tr - 1e-4 * scale).max())
+    else:
+        sig = np.linalg.svd(g["F"].reshape(-1, 3, 3).astype(np.float64), compute_uv=False)
+        eps = np.log(np.maximum(sig, 0.01))
+        dev = eps - eps.mean(axis=1, keepdims=True)
+        vm = 2 * mu * np.sqrt((dev * dev).sum(axis=1))
+        ys = g["yield_"].ravel().astype(np.float64)
+        assert vm.max() > 0.5 * sc.yield_stress  # the impact yielded the block
+        assert (vm <= ys * (1 + 1e-3)).all(), float((vm / ys).max())
+    e = sim._engine
+    e.stage("sort")
+    e.stage("p2g", dt=sc.dt)
+    gm, _, _ = e.export_grid(0)
+    mass = sc.particles()[3].astype(np.float64).sum()
+    assert abs(float(gm.double().sum()) / mass - 1) < 1e-5
