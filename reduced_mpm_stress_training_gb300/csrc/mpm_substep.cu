@@ -2,19 +2,21 @@
 //
 // Grid storage is block-major: the nodes of each 4x4x4 grid block are 64
 // consecutive float4 (momentum xyz + mass, or velocity xyz + mass), blocks
-// of all scenes concatenated.  Work is a list of "chunks": up to chunk_size
-// sorted particles that share one grid block of base cells, so all their
-// 3x3x3 stencils fall in the 6x6x6 node tile anchored at that block.
+// of all scenes concatenated.  The particles whose stencil base cells lie in
+// one grid block have all their 3x3x3 stencils in the 6x6x6 node tile
+// anchored at that block.
 //
-//   p2g  -- one CTA per chunk: accumulate the tile in shared memory with
-//           shared atomics, flush each non-zero node with ONE float4
-//           atomicAdd to global memory, and register the 8 grid blocks the
-//           tile covers in the active-block list.
+//   p2g  -- one warp per non-empty block: per-cell runs of particles summed
+//           in registers and added to a warp-private tile in shared memory,
+//           each non-zero node flushed with ONE float4 atomicAdd to global
+//           memory, and the 8 grid blocks the tile covers registered in the
+//           active-block list.
 //   grid -- one thread per node of each active block: momentum/mass +
 //           gravity, colliders in registration order; clears the block
 //           flag.  (The accumulator is zeroed by the next substep's
 //           scatter, so grid mass and momentum stay readable meanwhile.)
-//   g2p  -- one CTA per chunk: stage the tile of grid velocities in shared
+//   g2p  -- one CTA per chunk (up to chunk_size sorted particles of one
+//           block): stage the tile of grid velocities in shared
 //           memory, gather 27 nodes per particle, APIC C, velocity
 //           gradient, F update, return map + stress on one SVD, the
 //           displacement update and the cell key + histograms of the next
@@ -33,24 +35,41 @@ namespace mpm {
 // One warp per non-empty grid block, with a warp-private 6x6x6 node tile in
 // shared memory and no floating-point atomics in the particle loop.  The
 // sort delivers the block's particles ordered by cell with each cell's range
-// (cell_start .. cell_cursor).  The warp walks them "layer-major": layer r
-// holds the r-th particle of every cell, so a window of 32 consecutive
-// entries has (almost always) 32 distinct cells, whose stencils hit distinct
-// nodes for every node offset -- plain read-modify-writes of the tile are
-// race-free.  The rare lanes that share a cell (windows spanning two short
-// layers) are serialised by __match_any_sync rank.  A window reads 32 whole
-// particle records (128 B each, float4 loads), so the scattered order costs
-// no extra DRAM sectors.  The tile is flushed with one float4 atomicAdd per
-// non-zero node into the global grid.
+// (cell_start .. cell_cursor).  Particles of one cell share their 27 stencil
+// nodes, so a lane takes a run of consecutive particles of one cell, sums
+// their contributions in registers (27 nodes x 4 = 108 accumulators) and
+// adds them to the tile once: the shared-memory read-modify-writes drop
+// from one per particle and node to one per run and node.  A round gives
+// each lane a run of the same length L from a DISTINCT cell, whose stencils
+// hit distinct nodes for every node offset -- the tile updates are
+// race-free.  The cells are chosen longest-remaining first (every cell with
+// at least t particles left, t the smallest threshold that leaves at most 32
+// such cells, filled up to 32 with cells that have t - 1 left: Hu's list
+// schedule for chains), and L is the fewest particles any chosen cell has
+// left, at most kRunMax, so no lane idles inside a round.  Each lane streams
+// its run's 128-byte records into shared memory with cp.async one particle
+// ahead.  The tile is flushed with one
+// float4 atomicAdd per non-zero node into the global grid.
+//
+// Tile layout: rows of 6 nodes along z padded to 8 slots and rotated by
+// 4 (y & 1), so a node's 16-byte bank group is (z + 4 (y & 1)) mod 8: the 8
+// lanes of a quarter-warp (one 128-bit shared access phase) holding two
+// y-adjacent rows of 4 cells hit 8 distinct bank groups for every offset.
 // ---------------------------------------------------------------------------
 constexpr int kP2GWarps = 4;
-constexpr int kPassCap = 256;  // layer-major entries buffered per batch
+constexpr int kRunMax = 4;     // most particles of one cell a lane takes per round
 constexpr int kP2GQuads = 8;   // record quads P2G reads (q0-q7, 128 B)
+constexpr int kRowSlots = 8;
+constexpr int kP2GSlots = kTile * kTile * kRowSlots;
+
+__device__ __forceinline__ int p2g_slot(int x, int y, int z) {
+    return (x * kTile + y) * kRowSlots + ((z + 4 * (y & 1)) & 7);
+}
 
 struct P2GWarpSmem {
-    float4 tile[kTileNodes];
-    int perm[kPassCap];                 // record slots of the batch, layer-major
-    float4 rec[kP2GQuads][32];          // records of the next 32-particle window
+    float4 tile[kP2GSlots];
+    float4 rec[2][kP2GQuads][32];  // each lane's current and next record
+    int4 seg[32];                  // the round's runs: first sorted position, cell
 };
 
 struct P2GParticle {
@@ -100,12 +119,18 @@ __device__ __forceinline__ bool p2g_load(const MpmScene &S, const float4 (&q)[kP
     return true;
 }
 
-// add one particle's 27 node contributions into the tile (read-modify-write).
+// add one particle's 27 node contributions to the lane's accumulators
+// (x, y packed in axy, z and mass in azw: Blackwell's two-wide FP32 FMA).
 // Per (i,j) the node value factors over k:
 //   add_r = wz_k A_r + k wz_k B_r + dwz_k D_r,  mass = pm wz_k
 // with pm = wx_i wy_j m, A_r = pm (a0_r + i Cdx_r + j Cdy_r) + T_r0 dwx_i wy_j
 // + T_r1 wx_i dwy_j, B_r = pm Cdz_r, D_r = T_r2 wx_i wy_j.
-__device__ __forceinline__ void p2g_scatter(const P2GParticle &P, float4 *tile, unsigned mask) {
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+__device__ __forceinline__ void p2g_accumulate(const P2GParticle &P, float2 (&axy)[27], float2 (&azw)[27]) {
+    const float2 a0 = f2(P.a0[0], P.a0[1]);
+    const float2 cdx = f2(P.Cd[0], P.Cd[3]), cdy = f2(P.Cd[1], P.Cd[4]), cdz = f2(P.Cd[2], P.Cd[5]);
+    const float2 t0 = f2(P.T[0], P.T[3]), t1 = f2(P.T[1], P.T[4]), t2 = f2(P.T[2], P.T[5]);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
 #pragma unroll
@@ -114,28 +139,55 @@ __device__ __forceinline__ void p2g_scatter(const P2GParticle &P, float4 *tile, 
             const float p2 = P.W.w[0][i] * P.W.dw[1][j];
             const float p3 = P.W.w[0][i] * P.W.w[1][j];
             const float pm = p3 * P.m;
-            float A[3], B[3], D[3];
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                const float aij = P.a0[r] + (float)i * P.Cd[r * 3 + 0] + (float)j * P.Cd[r * 3 + 1];
-                A[r] = pm * aij + P.T[r * 3 + 0] * p1 + P.T[r * 3 + 1] * p2;
-                B[r] = pm * P.Cd[r * 3 + 2];
-                D[r] = P.T[r * 3 + 2] * p3;
-            }
-            float4 *t = tile + ((P.lx + i) * kTile + (P.ly + j)) * kTile + P.lz;
+            float2 aij = a0;
+            if (i > 0) aij = __ffma2_rn(f2((float)i, (float)i), cdx, aij);
+            if (j > 0) aij = __ffma2_rn(f2((float)j, (float)j), cdy, aij);
+            const float2 A = __ffma2_rn(f2(pm, pm), aij, __ffma2_rn(t0, f2(p1, p1), __fmul2_rn(t1, f2(p2, p2))));
+            const float2 B = __fmul2_rn(f2(pm, pm), cdz);
+            const float2 D = __fmul2_rn(t2, f2(p3, p3));
+            const float az = P.a0[2] + (float)i * P.Cd[6] + (float)j * P.Cd[7];
+            const float Az = pm * az + P.T[6] * p1 + P.T[7] * p2;
+            const float Bz = pm * P.Cd[8];
+            const float Dz = P.T[8] * p3;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const float wz = P.W.w[2][k], dwz = P.W.dw[2][k], kwz = (float)k * wz;
-                float4 o = t[k];
-                o.x += wz * A[0] + kwz * B[0] + dwz * D[0];
-                o.y += wz * A[1] + kwz * B[1] + dwz * D[1];
-                o.z += wz * A[2] + kwz * B[2] + dwz * D[2];
-                o.w += pm * wz;
-                t[k] = o;
-                __syncwarp(mask);
+                const float wz = P.W.w[2][k], dwz = P.W.dw[2][k];
+                float2 &xy = axy[(i * 3 + j) * 3 + k];
+                float2 &zw = azw[(i * 3 + j) * 3 + k];
+                xy = __ffma2_rn(f2(wz, wz), A, xy);
+                zw = __ffma2_rn(f2(wz, wz), f2(Az, pm), zw);
+                xy = __ffma2_rn(f2(dwz, dwz), D, xy);
+                zw.x = fmaf(dwz, Dz, zw.x);
+                if (k > 0) {
+                    const float kwz = k == 1 ? wz : 2.0f * wz;
+                    xy = __ffma2_rn(f2(kwz, kwz), B, xy);
+                    zw.x = fmaf(kwz, Bz, zw.x);
+                }
             }
         }
     }
+}
+
+// add a segment's accumulated nodes into the tile (read-modify-write; the
+// lanes of `mask` hold distinct cells)
+__device__ __forceinline__ void p2g_flush(const float2 (&axy)[27], const float2 (&azw)[27], int lx, int ly,
+                                          int lz, float4 *tile, unsigned mask) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float4 *t = tile + p2g_slot(lx + i, ly + j, lz + k);
+                const int n = (i * 3 + j) * 3 + k;
+                float4 o = *t;
+                o.x += axy[n].x;
+                o.y += axy[n].y;
+                o.z += azw[n].x;
+                o.w += azw[n].y;
+                *t = o;
+                __syncwarp(mask);
+            }
 }
 
 __device__ __forceinline__ void p2g_cp_async16(void *smem, const void *gmem) {
@@ -143,18 +195,66 @@ __device__ __forceinline__ void p2g_cp_async16(void *smem, const void *gmem) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
-// queue the record copies of window w of the batch (lane = entry)
-__device__ __forceinline__ void p2g_prefetch(P2GWarpSmem &sm, const PState &st, int w, int nv, int lane) {
-    const int k = w * 32 + lane;
-    if (k < nv) {
-        const float4 *src = st.rec + (int64_t)sm.perm[k] * kRecQuads;
+// queue the copy of one record (slot >= 0) into the lane's buffer b
+__device__ __forceinline__ void p2g_prefetch(P2GWarpSmem &sm, const PState &st, int slot, int b, int lane) {
+    if (slot >= 0) {
+        const float4 *src = st.rec + (int64_t)slot * kRecQuads;
 #pragma unroll
-        for (int q = 0; q < kP2GQuads; ++q) p2g_cp_async16(&sm.rec[q][lane], src + q);
+        for (int q = 0; q < kP2GQuads; ++q) p2g_cp_async16(&sm.rec[b][q][lane], src + q);
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kP2GWarps * 32, 5) p2g_kernel(const MpmScene *__restrict__ scenes,
+// Choose the next round of a block: up to 32 distinct cells, longest
+// remaining first, each giving its next L particles.  Lane `lane` owns cells
+// lane and lane + 32 (remaining counts rem0/rem1, next positions pos0/pos1).
+// Returns false when the block is done; else the lane's run (first sorted
+// position, cell, length len: L or 0) and the round length L.
+__device__ __forceinline__ bool p2g_next_round(int &rem0, int &rem1, int &pos0, int &pos1, int lane, unsigned lt,
+                                               int4 *seg, int &start, int &cell, int &len, int &L) {
+    const unsigned full = 0xffffffffu;
+    const int maxrem = __reduce_max_sync(full, max(rem0, rem1));
+    if (maxrem == 0) return false;
+    // smallest t >= 1 with at most 32 cells holding >= t particles
+    int lo = 1, hi = maxrem + 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const int cnt = __popc(__ballot_sync(full, rem0 >= mid)) + __popc(__ballot_sync(full, rem1 >= mid));
+        if (cnt <= 32) hi = mid;
+        else lo = mid + 1;
+    }
+    const unsigned h0 = __ballot_sync(full, rem0 >= lo), h1 = __ballot_sync(full, rem1 >= lo);
+    const int need = 32 - __popc(h0) - __popc(h1);
+    const unsigned f0 = __ballot_sync(full, lo > 1 && rem0 == lo - 1);
+    const unsigned f1 = __ballot_sync(full, lo > 1 && rem1 == lo - 1);
+    const bool p0 = rem0 >= lo || (((f0 >> lane) & 1u) && __popc(f0 & lt) < need);
+    const bool p1 = rem1 >= lo || (((f1 >> lane) & 1u) && __popc(f0) + __popc(f1 & lt) < need);
+    const unsigned b0 = __ballot_sync(full, p0), b1 = __ballot_sync(full, p1);
+    // every chosen cell gives its next L particles, L = the fewest any of them has left
+    const unsigned least =
+        __reduce_min_sync(full, min(p0 ? (unsigned)rem0 : 0xffffffffu, p1 ? (unsigned)rem1 : 0xffffffffu));
+    L = min((int)least, kRunMax);
+    if (p0) {
+        seg[__popc(b0 & lt)] = make_int4(pos0, lane, 0, 0);
+        pos0 += L;
+        rem0 -= L;
+    }
+    if (p1) {
+        seg[__popc(b0) + __popc(b1 & lt)] = make_int4(pos1, lane + 32, 0, 0);
+        pos1 += L;
+        rem1 -= L;
+    }
+    const int tot = __popc(b0) + __popc(b1);
+    __syncwarp();
+    const int4 mine = lane < tot ? seg[lane] : make_int4(0, 0, 0, 0);
+    __syncwarp();  // seg[] is rewritten by the next call
+    start = mine.x;
+    cell = mine.y;
+    len = lane < tot ? L : 0;
+    return true;
+}
+
+__global__ void __launch_bounds__(kP2GWarps * 32, 2) p2g_kernel(const MpmScene *__restrict__ scenes,
                                                                 PState st, Ws ws, float dt,
                                                                 int *status) {
     extern __shared__ __align__(16) unsigned char p2g_smem_raw[];
@@ -170,67 +270,81 @@ __global__ void __launch_bounds__(kP2GWarps * 32, 5) p2g_kernel(const MpmScene *
         const MpmScene &S = scenes[be.w];
         int bx, by, bz;
         chunk_block(S, be.x, bx, by, bz);
-        for (int i = lane; i < kTileNodes; i += 32) sm.tile[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = lane; i < kP2GSlots; i += 32) sm.tile[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         // cell ranges of this block: lane owns cells lane and lane + 32
         const int64_t cb = (int64_t)be.x * 64;
         const int s0 = ws.cell_start[cb + lane], s1 = ws.cell_start[cb + lane + 32];
         const int c0 = max(0, ws.cell_cursor[cb + lane] - s0);
         const int c1 = max(0, ws.cell_cursor[cb + lane + 32] - s1);
-        const int maxcnt = __reduce_max_sync(full, max(c0, c1));
-        int r = 0;
-        while (r < maxcnt) {
-            // layer-major batch: whole layers while they fit in the buffer
-            int nv = 0;
-            while (r < maxcnt && nv <= kPassCap - 64) {
-                const bool a = c0 > r, b = c1 > r;
-                const unsigned ma = __ballot_sync(full, a), mb = __ballot_sync(full, b);
-                // sorted positions come from the block's cell ranges (< n); store their slots
-                if (a) sm.perm[nv + __popc(ma & lt)] = ws.order[s0 + r];
-                if (b) sm.perm[nv + __popc(ma) + __popc(mb & lt)] = ws.order[s1 + r];
-                nv += __popc(ma) + __popc(mb);
-                ++r;
-            }
-            __syncwarp();
-            // windows of 32 entries; once window w is in registers, the records
-            // of window w + 1 stream into the shared buffer while w is scattered
-            const int nwin = (nv + 31) >> 5;
-            if (nwin > 0) p2g_prefetch(sm, st, 0, nv, lane);
-            for (int w = 0; w < nwin; ++w) {
-                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-                __syncwarp();
-                const int k = w * 32 + lane;
-                bool act = k < nv;
-                float4 q[kP2GQuads];
-                if (act) {
+        // Rounds are software-pipelined: while round A is summed, round B is
+        // chosen and its order[] entries load, and A's last iteration already
+        // streams B's first records.
+        int rem0 = c0, rem1 = c1, pos0 = s0, pos1 = s1;
+        int startA, cellA, lenA, LA;
+        bool haveA = p2g_next_round(rem0, rem1, pos0, pos1, lane, lt, sm.seg, startA, cellA, lenA, LA);
+        int slA[kRunMax];
 #pragma unroll
-                    for (int qq = 0; qq < kP2GQuads; ++qq) q[qq] = sm.rec[qq][lane];
-                }
-                __syncwarp();
-                if (w + 1 < nwin) p2g_prefetch(sm, st, w + 1, nv, lane);
-                P2GParticle P;
-                if (act) {
-                    act = p2g_load(S, q, bx, by, bz, dt, P);
-                    if (!act) atomicOr(status, MPM_ST_INTERNAL);
-                }
-                const int cell = act ? (P.lx * 4 + P.ly) * 4 + P.lz : -1 - lane;
-                const unsigned peers = __match_any_sync(full, cell);
-                const int rank = act ? __popc(peers & lt) : 0;
-                const int npass = __reduce_max_sync(full, rank) + 1;
-                for (int q = 0; q < npass; ++q) {
-                    const bool go = act && rank == q;
-                    const unsigned gm = __ballot_sync(full, go);
-                    if (go) p2g_scatter(P, sm.tile, gm);
-                    __syncwarp();
+        for (int t = 0; t < kRunMax; ++t) slA[t] = t < lenA ? ws.order[startA + t] : -1;  // positions < n
+        int buf = 0;
+        if (haveA) p2g_prefetch(sm, st, slA[0], 0, lane);
+        bool bad = false;
+        while (haveA) {
+            int startB, cellB, lenB, LB;
+            const bool haveB = p2g_next_round(rem0, rem1, pos0, pos1, lane, lt, sm.seg, startB, cellB, lenB, LB);
+            int slB[kRunMax];
+#pragma unroll
+            for (int t = 0; t < kRunMax; ++t) slB[t] = haveB && t < lenB ? ws.order[startB + t] : -1;
+            const int cx = cellA >> 4, cy = (cellA >> 2) & 3, cz = cellA & 3;
+            float2 axy[27], azw[27];
+#pragma unroll
+            for (int k = 0; k < 27; ++k) {
+                axy[k] = make_float2(0.f, 0.f);
+                azw[k] = make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int t = 0; t < kRunMax; ++t) {
+                if (t < LA) {  // warp-uniform
+                    // the next record (this run's, or the next round's first) streams in
+                    // while this one is summed
+                    int nxt = slB[0];
+#pragma unroll
+                    for (int u = 0; u + 1 < kRunMax; ++u)
+                        if (u == t && t + 1 < LA) nxt = slA[u + 1];
+                    p2g_prefetch(sm, st, nxt, buf ^ 1, lane);
+                    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+                    if (t < lenA) {
+                        float4 q[kP2GQuads];
+#pragma unroll
+                        for (int qq = 0; qq < kP2GQuads; ++qq) q[qq] = sm.rec[buf][qq][lane];
+                        P2GParticle P;
+                        const bool ok =
+                            p2g_load(S, q, bx, by, bz, dt, P) && P.lx == cx && P.ly == cy && P.lz == cz;
+                        if (ok) p2g_accumulate(P, axy, azw);
+                        bad |= !ok;
+                    }
+                    buf ^= 1;
                 }
             }
-            __syncwarp();  // perm and the record buffers are refilled by the next batch
+            const unsigned fm = __ballot_sync(full, lenA > 0);
+            if (lenA > 0) p2g_flush(axy, azw, cx, cy, cz, sm.tile, fm);
+            __syncwarp();
+            haveA = haveB;
+            startA = startB;
+            cellA = cellB;
+            lenA = lenB;
+            LA = LB;
+#pragma unroll
+            for (int t = 0; t < kRunMax; ++t) slA[t] = slB[t];
         }
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        if (bad) atomicOr(status, MPM_ST_INTERNAL);
         // flush the tile: one float4 atomic per non-zero node
         const int nb = S.n_blocks_axis;
-        for (int i = lane; i < kTileNodes; i += 32) {
+        for (int i = lane; i < kP2GSlots; i += 32) {
             const float4 a = sm.tile[i];
             if (a.x != 0.0f || a.y != 0.0f || a.z != 0.0f || a.w != 0.0f) {
-                const int tx = i / 36, ty = (i / 6) % 6, tz = i % 6;
+                const int tx = i / (kTile * kRowSlots), ty = (i / kRowSlots) % kTile;
+                const int tz = ((i & 7) - 4 * (ty & 1)) & 7;  // unused slots (tz 6, 7) stay zero
                 const int ix = 4 * bx + tx, iy = 4 * by + ty, iz = 4 * bz + tz;
                 if (ix < S.n_grid && iy < S.n_grid && iz < S.n_grid)
                     atomicAdd(ws.grid_acc + node_addr(S.block_begin, nb, ix, iy, iz), a);
@@ -598,9 +712,11 @@ cudaError_t launch_p2g(const Ctx &cx, float dt) {
         if (e != cudaSuccess) return e;
         if (dev >= 0 && dev < 64) attr_set[dev] = true;
     }
-    // persistent: five CTAs (20 warps) per SM, never more warps than blocks
+    // up to eight CTAs (32 warps) per SM, several times the resident ones:
+    // the rest start as others finish, which balances blocks of unequal size;
+    // warps loop over blocks when there are more blocks than warps
     int64_t want = (cx.total_blocks + kP2GWarps - 1) / kP2GWarps;
-    int grid = (int)(want < (int64_t)cx.num_sms * 5 ? want : (int64_t)cx.num_sms * 5);
+    int grid = (int)(want < (int64_t)cx.num_sms * 8 ? want : (int64_t)cx.num_sms * 8);
     if (grid < 1) grid = 1;
     p2g_kernel<<<grid, kP2GWarps * 32, bytes, cx.stream>>>(cx.scenes, cx.st, cx.ws, dt, cx.status);
     return cudaGetLastError();
