@@ -336,14 +336,16 @@ int mpm_adjoint_substep(MpmBuffers *b, const float *adj_out, float *adj_in, void
                         double *theta_bar, float time, float dt, void *stream);
 
 /* Saved grids for the reverse pass (checkpointing with recompute).  The
- * reverse pass of a substep reads its sorted order, its active-block list
- * and those blocks' grid momentum + mass and velocity.  mpm_save_substep_grid
- * copies them (active blocks only) into a device blob of
- * mpm_substep_grid_bytes(plan) bytes (256-byte aligned) right after the
- * substep's mpm_grid_update; mpm_load_substep_grid puts them back before
- * mpm_adjoint_substep, which then needs no new sort, P2G or grid update.
- * Loading leaves grid blocks of other substeps in the accumulator:
- * mpm_clear_grid empties it (call it before stepping forward again). */
+ * reverse pass of a substep and the substep's G2P read its sorted order, its
+ * active-block list, its G2P chunk list and those blocks' grid momentum +
+ * mass and velocity.  mpm_save_substep_grid copies them (active blocks
+ * only) into a device blob of mpm_substep_grid_bytes(plan) bytes (256-byte
+ * aligned) right after the substep's mpm_grid_update; mpm_load_substep_grid
+ * puts them back, after which mpm_adjoint_substep -- or mpm_g2p, to rebuild
+ * the state after the substep from the state before it -- needs no new
+ * sort, P2G or grid update.  Loading leaves grid blocks of other substeps in
+ * the accumulator: mpm_clear_grid empties it (call it before stepping
+ * forward again). */
 int64_t mpm_substep_grid_bytes(const MpmPlan *plan);
 int mpm_save_substep_grid(MpmBuffers *b, void *dst, void *stream);
 int mpm_load_substep_grid(MpmBuffers *b, const void *src, void *stream);

@@ -5,12 +5,16 @@ The reference has no gradient path (no ``wp.Tape``); this module adds one
 for the substep it replaces (engine_stress/mpm_solver_warp.py:156-203).
 ``SandRollout.forward`` advances a sand scene from an initial velocity field
 and a material (E, friction angle), keeping a checkpoint of the particle
-state every ``checkpoint_every`` substeps.  ``SandRollout.backward`` walks
-the segments newest first: it restores a segment's checkpoint, recomputes
-the segment's states, and for each substep (newest first) rebuilds that
-substep's grid (sort, P2G, grid update) and calls ``mpm_adjoint_substep``,
-which runs the reverse G2P (with the return-map adjoint), the reverse grid
-update and the reverse P2G on the device.  The adjoints of the initial
+state every ``checkpoint_every`` substeps and, with ``grid_tape`` (the
+default), each substep's grid (``mpm_save_substep_grid``: sorted order,
+chunk list, active blocks' momentum, mass and velocity).
+``SandRollout.backward`` walks the segments newest first: it restores a
+segment's checkpoint and recomputes the segment's states -- with the grid
+tape by G2P alone from each substep's saved grid, without it by the whole
+substep (sort, P2G, grid update, G2P), saving the grids on the way -- then
+for each substep (newest first) loads its grid and calls
+``mpm_adjoint_substep``, which runs the reverse G2P (with the return-map
+adjoint), the reverse grid update and the reverse P2G on the device.  The adjoints of the initial
 velocity and of (mu, lam, alpha) come out; the chain rule to E and the
 friction angle is applied here.
 
@@ -38,10 +42,13 @@ class SandRollout:
     """One sand scene, rolled out and differentiated on one device."""
 
     def __init__(self, scene: Scene, n_substeps: int | None = None, checkpoint_every: int = 10,
-                 device="cuda:0", chunk_size: int = 128, particles=None, initial: dict | None = None):
+                 device="cuda:0", chunk_size: int = 128, particles=None, initial: dict | None = None,
+                 grid_tape: bool = True):
         """particles: (x0, v0, vol, mass) arrays overriding the scene's sampling;
         initial: {field id: (n, comps) tensor} loaded after them (e.g. a
-        prestrained F with its stress)."""
+        prestrained F with its stress); grid_tape: keep every substep's grid
+        from the forward pass (n_substeps x mpm_substep_grid_bytes of device
+        memory) so the backward pass recomputes states by G2P alone."""
         if scene.material != "sand":
             raise ValueError("the adjoint covers sand (Drucker-Prager) scenes only")
         if checkpoint_every < 1:
@@ -68,6 +75,8 @@ class SandRollout:
         self.grid_adj = torch.empty(self.engine.plan.total_blocks * 64 * 4, dtype=torch.float32, device=dev)
         self.theta_bar = torch.zeros(3, dtype=torch.float64, device=dev)
         self.adj = [torch.zeros(self.n * A.ADJ_WORDS, dtype=torch.float32, device=dev) for _ in range(2)]
+        self.grid_tape = bool(grid_tape)
+        self.tape = None
         self.k = int(checkpoint_every)
         self.E = float(scene.E)
         self.friction_angle = float(scene.friction_angle)
@@ -80,7 +89,8 @@ class SandRollout:
     @k.setter
     def k(self, k: int) -> None:
         """Allocate the checkpoint storage: one state buffer per checkpoint,
-        k + 1 state buffers for a recomputed segment, k saved grids."""
+        k + 1 state buffers for a recomputed segment, and k saved grids when
+        there is no grid tape."""
         k = int(k)
         if k < 1:
             raise ValueError("checkpoint interval must be >= 1")
@@ -92,7 +102,9 @@ class SandRollout:
         n_ckpt = (self.n_substeps + k - 1) // k
         self.checkpoints = [torch.empty(sb, dtype=torch.uint8, device=dev) for _ in range(n_ckpt)]
         self.pool = [torch.empty(sb, dtype=torch.uint8, device=dev) for _ in range(k + 1)]
-        self.grids = [torch.empty(gb, dtype=torch.uint8, device=dev) for _ in range(k)]
+        self.grids = None if self.grid_tape else [torch.empty(gb, dtype=torch.uint8, device=dev) for _ in range(k)]
+        if self.grid_tape and self.tape is None:
+            self.tape = [torch.empty(gb, dtype=torch.uint8, device=dev) for _ in range(self.n_substeps)]
         self.have_checkpoints = False
         self._k = k
 
@@ -128,7 +140,15 @@ class SandRollout:
         for step in range(self.n_substeps):
             if keep and step % self.k == 0:
                 self.checkpoints[step // self.k].copy_(e._state[b.cur])
-            e.substep_raw(self.time_of(step), self.dt)
+            if keep and self.grid_tape:
+                t = self.time_of(step)
+                e.stage("sort")
+                e.stage("p2g", dt=self.dt)
+                e.stage("grid", time=t, dt=self.dt)
+                self._call("mpm_save_substep_grid", self.tape[step].data_ptr())
+                e.stage("g2p", dt=self.dt)
+            else:
+                e.substep_raw(self.time_of(step), self.dt)
         self.have_checkpoints = keep
         return e.export(A.FIELD_U).reshape(self.n, 3)
 
@@ -149,9 +169,10 @@ class SandRollout:
 
         Per segment (newest first): the segment's states are recomputed from
         its checkpoint straight into ``pool`` (G2P writes each new state into
-        the next pool buffer: no copies), each substep's grid is saved after
-        its grid update, then the substeps are reversed newest first from
-        their pool state and saved grid."""
+        the next pool buffer: no copies) -- from the grid tape by G2P alone,
+        otherwise by whole substeps whose grids are saved after their grid
+        update -- then the substeps are reversed newest first from their pool
+        state and saved grid."""
         if not self.have_checkpoints:
             raise RuntimeError("run forward(keep=True) first")
         e = self.engine
@@ -178,6 +199,11 @@ class SandRollout:
                     t = self.time_of(start + j)
                     if j + 1 < L:
                         b.state[b.cur ^ 1] = self.pool[j + 1].data_ptr()
+                    if self.grid_tape:
+                        if j + 1 < L:
+                            self._call("mpm_load_substep_grid", self.tape[start + j].data_ptr())
+                            e.stage("g2p", dt=self.dt)
+                        continue
                     e.stage("sort")
                     e.stage("p2g", dt=self.dt)
                     e.stage("grid", time=t, dt=self.dt)
@@ -186,7 +212,8 @@ class SandRollout:
                         e.stage("g2p", dt=self.dt)
                 for j in reversed(range(L)):
                     b.state[b.cur] = self.pool[j].data_ptr()
-                    self._call("mpm_load_substep_grid", self.grids[j].data_ptr())
+                    blob = self.tape[start + j] if self.grid_tape else self.grids[j]
+                    self._call("mpm_load_substep_grid", blob.data_ptr())
                     A.check(self.lib.mpm_adjoint_substep(C.byref(b), out.data_ptr(), inp.data_ptr(),
                                                          self.grid_adj.data_ptr(), self.theta_bar.data_ptr(),
                                                          self.time_of(start + j), self.dt, _stream(self.device)),

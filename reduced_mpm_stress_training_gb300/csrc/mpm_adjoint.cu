@@ -417,10 +417,9 @@ __global__ void __launch_bounds__(128) g2p_adjoint_kernel(const MpmScene *__rest
                                 c4 * nw.w * (nCb[r * 3 + 0] * dpos[0] + nCb[r * 3 + 1] * dpos[1] + nCb[r * 3 + 2] * dpos[2]) +
                                 nFb[r * 3 + 0] * nw.dw[0] + nFb[r * 3 + 1] * nw.dw[1] + nFb[r * 3 + 2] * nw.dw[2];
                     }
-                    float4 *dst = grid_adj + node_addr(S.block_begin, nb, p.base[0] + i, p.base[1] + j, p.base[2] + k);
-                    atomicAdd(&dst->x, gb[0]);
-                    atomicAdd(&dst->y, gb[1]);
-                    atomicAdd(&dst->z, gb[2]);
+                    // one vector atomic per node (w, unused until the grid adjoint overwrites it, gets 0)
+                    atomicAdd(grid_adj + node_addr(S.block_begin, nb, p.base[0] + i, p.base[1] + j, p.base[2] + k),
+                              make_float4(gb[0], gb[1], gb[2], 0.0f));
                     // particle position adjoint through the weights and dpos
                     const float gvb = nvb[0] * g[0] + nvb[1] * g[1] + nvb[2] * g[2];
                     float qv[3], sv[3];

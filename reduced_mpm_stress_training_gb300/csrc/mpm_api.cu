@@ -361,7 +361,7 @@ int mpm_adjoint_substep(MpmBuffers *b, const float *adj_out, float *adj_in, void
 
 int64_t mpm_substep_grid_bytes(const MpmPlan *plan) {
     if (!plan) return -1;
-    return mpm::substep_grid_bytes(plan->total_blocks, plan->n_particles);
+    return mpm::substep_grid_bytes(plan->total_blocks, plan->n_particles, plan->max_chunks);
 }
 
 int mpm_save_substep_grid(MpmBuffers *b, void *dst, void *stream) {

@@ -45,7 +45,7 @@ cudaError_t launch_adjoint(const Ctx &cx, const float *adj_out, float *adj_in, f
 cudaError_t launch_return_map_vjp(const MpmScene &scene, const float *Ft, const float *Fb, const float *Tb,
                                   float *Ftb, double *thb, int64_t n, cudaStream_t st);
 // saved grids for the reverse pass (mpm_checkpoint.cu)
-int64_t substep_grid_bytes(int64_t total_blocks, int64_t n);
+int64_t substep_grid_bytes(int64_t total_blocks, int64_t n, int64_t max_chunks);
 cudaError_t launch_save_grid(const Ctx &cx, void *dst);
 cudaError_t launch_load_grid(const Ctx &cx, const void *src);
 cudaError_t launch_clear_grid(const Ctx &cx);
