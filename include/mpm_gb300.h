@@ -165,6 +165,27 @@ int mpm_load(MpmBuffers *b, int32_t field, const float *src, int32_t src_on_host
  * Replaces export_uvFstress_from_warp (:305-310) and the wp.array reads of
  * mpm_state.particle_* (e.g. save_data_at_frame :351-384). */
 int mpm_export(MpmBuffers *b, int32_t field, float *dst, int32_t dst_on_host, void *stream);
+/* load_uvstress_from_tensor (engine_stress/mpm_solver_warp.py:253-266) in one
+ * pass: u (n,3), v (n,3), stress (n,9), user order, host (pinned) or device.
+ * From the host the copy runs on a library side stream that waits only for
+ * the previous mpm_load_uvstress to have consumed its staging, so it may
+ * overlap earlier work on `stream` and an mpm_export_uvFstress copy in
+ * flight; the load itself is ordered on `stream`.  The host arrays must stay
+ * unchanged until `stream` reaches the load. */
+int mpm_load_uvstress(MpmBuffers *b, const float *u, const float *v, const float *stress, int32_t src_on_host,
+                      void *stream);
+/* export_uvFstress_from_warp (engine_stress/mpm_solver_warp.py:305-310) in one
+ * pass: u (n,3), v (n,3), F_disp = F - I (n,9), stress (n,9) in user order.
+ * dst_on_host 0: device arrays, ordered on `stream`.  1: host (pinned)
+ * arrays, the call returns after the copies landed.  2: host arrays, the
+ * copies run on a library side stream after the export kernel and may
+ * overlap later work on `stream`; read the arrays after mpm_sync_transfers()
+ * or a device synchronize. */
+int mpm_export_uvFstress(MpmBuffers *b, float *u, float *v, float *F_disp, float *stress, int32_t dst_on_host,
+                         void *stream);
+/* Waits (host) for every host copy mpm_load_uvstress / mpm_export_uvFstress
+ * left in flight on the current device. */
+int mpm_sync_transfers(void);
 
 /* ---- the substep ----------------------------------------------------- */
 

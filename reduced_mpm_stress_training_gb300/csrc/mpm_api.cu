@@ -71,7 +71,9 @@ WsLayout ws_layout(const MpmPlan &p) {
     L.active_list = take(p.total_blocks * 4);
     L.n_active = take(4);
     L.n_active_prev = take(4);
-    L.staging = take(n * 9 * 4);
+    // host transfers: [u, v, stress in: 15 n][u, v, F_disp, stress out: 24 n] (disjoint, so the
+    // next step's input copy may run while this step's output copy is in flight)
+    L.staging = take(n * 39 * 4);
     L.total = o;
     return L;
 }
@@ -244,6 +246,96 @@ int mpm_export(MpmBuffers *b, int32_t field, float *dst, int32_t dst_on_host, vo
         if (bytes) MPM_CHECK(cudaMemcpyAsync(dst, to, bytes, cudaMemcpyDeviceToHost, cx.stream));
         MPM_CHECK(cudaStreamSynchronize(cx.stream));
     }
+    return MPM_OK;
+}
+
+// Side streams per device for the host copies of mpm_load_uvstress (input
+// lane) and mpm_export_uvFstress (output lane), and the events that order
+// them against the caller's stream.  An input copy waits only until the
+// previous load kernel has consumed the input staging; an output copy waits
+// for its export kernel, and the next export kernel waits for it to have
+// drained the output staging.  So the input copy of one step, the output copy
+// of the step before and the substep itself can all run at once.
+namespace {
+struct CopyLane {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ready = nullptr, done = nullptr;
+};
+CopyLane g_in[64], g_out[64];
+
+cudaError_t lane_of(CopyLane *lanes, CopyLane *&lane) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    CopyLane &L = lanes[dev];
+    if (!L.stream) {
+        if ((e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking)) != cudaSuccess) return e;
+        if ((e = cudaEventCreateWithFlags(&L.ready, cudaEventDisableTiming)) != cudaSuccess) return e;
+        if ((e = cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming)) != cudaSuccess) return e;
+    }
+    lane = &L;
+    return cudaSuccess;
+}
+}  // namespace
+
+int mpm_sync_transfers(void) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MPM_ERR_CUDA;
+    for (CopyLane *L : {&g_in[dev], &g_out[dev]})
+        if (L->stream) MPM_CHECK(cudaStreamSynchronize(L->stream));
+    return MPM_OK;
+}
+
+int mpm_load_uvstress(MpmBuffers *b, const float *u, const float *v, const float *stress, int32_t src_on_host,
+                      void *stream) {
+    if (!buffers_ok(b) || (b->plan.n_particles > 0 && (!u || !v || !stress))) return MPM_ERR_ARG;
+    mpm::Ctx cx = make_ctx(b, stream, b->cur);
+    if (cx.n == 0) return MPM_OK;
+    if (!src_on_host) {
+        MPM_CHECK(mpm::launch_load_uvstress(cx, u, v, stress));
+        b->keys_valid = 0;  // u moved the particles
+        return MPM_OK;
+    }
+    const size_t n = (size_t)cx.n;
+    float *s = cx.ws.staging;  // input region: u, v, stress
+    CopyLane *L = nullptr;
+    MPM_CHECK(lane_of(g_in, L));
+    MPM_CHECK(cudaStreamWaitEvent(L->stream, L->done, 0));  // no-op before the first load
+    MPM_CHECK(cudaMemcpyAsync(s, u, n * 12, cudaMemcpyHostToDevice, L->stream));
+    MPM_CHECK(cudaMemcpyAsync(s + 3 * n, v, n * 12, cudaMemcpyHostToDevice, L->stream));
+    MPM_CHECK(cudaMemcpyAsync(s + 6 * n, stress, n * 36, cudaMemcpyHostToDevice, L->stream));
+    MPM_CHECK(cudaEventRecord(L->ready, L->stream));
+    MPM_CHECK(cudaStreamWaitEvent(cx.stream, L->ready, 0));
+    MPM_CHECK(mpm::launch_load_uvstress(cx, s, s + 3 * n, s + 6 * n));
+    MPM_CHECK(cudaEventRecord(L->done, cx.stream));  // input staging consumed
+    b->keys_valid = 0;
+    return MPM_OK;
+}
+
+int mpm_export_uvFstress(MpmBuffers *b, float *u, float *v, float *F_disp, float *stress, int32_t dst_on_host,
+                         void *stream) {
+    if (!buffers_ok(b) || (b->plan.n_particles > 0 && (!u || !v || !F_disp || !stress))) return MPM_ERR_ARG;
+    mpm::Ctx cx = make_ctx(b, stream, b->cur);
+    if (cx.n == 0) return MPM_OK;
+    const size_t n = (size_t)cx.n;
+    float *s = cx.ws.staging + 15 * n;  // output region: u, v, F_disp, stress
+    if (!dst_on_host) {
+        MPM_CHECK(mpm::launch_export_uvFstress(cx, u, v, F_disp, stress));
+        return MPM_OK;
+    }
+    CopyLane *L = nullptr;
+    MPM_CHECK(lane_of(g_out, L));
+    MPM_CHECK(cudaStreamWaitEvent(cx.stream, L->done, 0));  // previous output copy drained the staging
+    MPM_CHECK(mpm::launch_export_uvFstress(cx, s, s + 3 * n, s + 6 * n, s + 15 * n));
+    MPM_CHECK(cudaEventRecord(L->ready, cx.stream));
+    MPM_CHECK(cudaStreamWaitEvent(L->stream, L->ready, 0));
+    MPM_CHECK(cudaMemcpyAsync(u, s, n * 12, cudaMemcpyDeviceToHost, L->stream));
+    MPM_CHECK(cudaMemcpyAsync(v, s + 3 * n, n * 12, cudaMemcpyDeviceToHost, L->stream));
+    MPM_CHECK(cudaMemcpyAsync(F_disp, s + 6 * n, n * 36, cudaMemcpyDeviceToHost, L->stream));
+    MPM_CHECK(cudaMemcpyAsync(stress, s + 15 * n, n * 36, cudaMemcpyDeviceToHost, L->stream));
+    MPM_CHECK(cudaEventRecord(L->done, L->stream));
+    if (dst_on_host == 1) MPM_CHECK(cudaEventSynchronize(L->done));
     return MPM_OK;
 }
 

@@ -67,6 +67,41 @@ __global__ void export_kernel(PState st, int n, int field, int nc, float *__rest
     }
 }
 
+// load_uvstress_from_tensor (mpm_solver_warp.py:253-266) in one pass: u, v
+// and stress of each slot's user particle into its record (quads 2, 3, 5-7;
+// the C words sharing quads 3 and 5 are kept)
+__global__ void load_uvstress_kernel(PState st, int n, const float *__restrict__ u, const float *__restrict__ v,
+                                     const float *__restrict__ tau) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t id = __float_as_int(ldrec(st, i, 1).y);
+    const float4 q3 = ldrec(st, i, 3), q5 = ldrec(st, i, 5);
+    const float *pu = u + id * 3, *pv = v + id * 3, *pt = tau + id * 9;
+    strec(st, i, 2, make_float4(pu[0], pu[1], pu[2], pv[0]));
+    strec(st, i, 3, make_float4(pv[1], pv[2], q3.z, q3.w));
+    strec(st, i, 5, make_float4(q5.x, q5.y, q5.z, pt[0]));
+    strec(st, i, 6, make_float4(pt[1], pt[2], pt[3], pt[4]));
+    strec(st, i, 7, make_float4(pt[5], pt[6], pt[7], pt[8]));
+}
+
+// export_uvFstress_from_warp (mpm_solver_warp.py:305-310) in one pass: u, v,
+// F - I (:16-19) and stress of each slot, written at its user index
+__global__ void export_uvFstress_kernel(PState st, int n, float *__restrict__ u, float *__restrict__ v,
+                                        float *__restrict__ fd, float *__restrict__ tau) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 q1 = ldrec(st, i, 1), q2 = ldrec(st, i, 2), q3 = ldrec(st, i, 3), q5 = ldrec(st, i, 5),
+                 q6 = ldrec(st, i, 6), q7 = ldrec(st, i, 7), q8 = ldrec(st, i, 8), q9 = ldrec(st, i, 9);
+    const int64_t id = __float_as_int(q1.y);
+    float *pu = u + id * 3, *pv = v + id * 3, *pf = fd + id * 9, *pt = tau + id * 9;
+    pu[0] = q2.x; pu[1] = q2.y; pu[2] = q2.z;
+    pv[0] = q2.w; pv[1] = q3.x; pv[2] = q3.y;
+    pf[0] = q8.x - 1.0f; pf[1] = q8.y; pf[2] = q8.z; pf[3] = q8.w; pf[4] = q9.x - 1.0f;
+    pf[5] = q9.y; pf[6] = q9.z; pf[7] = q9.w; pf[8] = q1.w - 1.0f;
+    pt[0] = q5.w; pt[1] = q6.x; pt[2] = q6.y; pt[3] = q6.z; pt[4] = q6.w;
+    pt[5] = q7.x; pt[6] = q7.y; pt[7] = q7.z; pt[8] = q7.w;
+}
+
 // dense (n,n,n) grid_m / grid_v_in from the accumulator (valid after p2g)
 __global__ void export_acc_kernel(const float4 *__restrict__ acc, int64_t block_begin, int nb, int n,
                                   float *gm, float *gvin) {
@@ -147,6 +182,18 @@ cudaError_t launch_export(const Ctx &cx, int field, float *dst) {
     if (cx.n == 0) return cudaSuccess;
     export_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, field,
                                                                  field_components(field), dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_load_uvstress(const Ctx &cx, const float *u, const float *v, const float *tau) {
+    if (cx.n == 0) return cudaSuccess;
+    load_uvstress_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, u, v, tau);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_uvFstress(const Ctx &cx, float *u, float *v, float *fd, float *tau) {
+    if (cx.n == 0) return cudaSuccess;
+    export_uvFstress_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, u, v, fd, tau);
     return cudaGetLastError();
 }
 

@@ -254,6 +254,44 @@ class MPMEngine:
                                     self.stream), "mpm_export")
         return out
 
+    def load_uvstress(self, u: torch.Tensor, v: torch.Tensor, stress: torch.Tensor) -> None:
+        """u (n,3), v (n,3), stress (n,3,3) in one pass (mpm_load_uvstress):
+        straight from pinned float32 host tensors through the staging copy,
+        anything else by way of device tensors."""
+        n = self.n_particles
+        ts = (u, v, stress)
+        if all(t.device.type == "cpu" and t.is_pinned() and t.dtype == torch.float32 and t.is_contiguous()
+               and t.numel() == n * c for t, c in zip(ts, (3, 3, 9))):
+            ts = [t.reshape(-1) for t in ts]
+            A.check(self.lib.mpm_load_uvstress(C.byref(self.buf), ts[0].data_ptr(), ts[1].data_ptr(),
+                                               ts[2].data_ptr(), 1, self.stream), "mpm_load_uvstress")
+            return
+        src = [self._as_input(t, c) for t, c in zip((u, v, stress), (3, 3, 9))]
+        A.check(self.lib.mpm_load_uvstress(C.byref(self.buf), src[0].data_ptr(), src[1].data_ptr(),
+                                           src[2].data_ptr(), 0, self.stream), "mpm_load_uvstress")
+
+    def export_uvFstress(self, out: tuple | None = None, wait: bool = True) -> tuple:
+        """(u, v, F_disp, stress) flat float32 tensors in one pass
+        (mpm_export_uvFstress): into `out` (four device tensors, or four
+        pinned host tensors of n*3, n*3, n*9, n*9 floats) or new device ones.
+        Host tensors with wait=False are filled asynchronously: call
+        ``sync_transfers()`` (or synchronize the device) before reading them."""
+        n = self.n_particles
+        if out is None:
+            out = tuple(torch.empty(n * c, dtype=torch.float32, device=self.device) for c in (3, 3, 9, 9))
+        on_host = out[0].device.type == "cpu"
+        for t, c in zip(out, (3, 3, 9, 9)):
+            assert t.dtype == torch.float32 and t.is_contiguous() and t.numel() == n * c
+            assert (t.device.type == "cpu") == on_host
+        mode = (1 if wait else 2) if on_host else 0
+        A.check(self.lib.mpm_export_uvFstress(C.byref(self.buf), *(t.data_ptr() for t in out), mode,
+                                              self.stream), "mpm_export_uvFstress")
+        return out
+
+    def sync_transfers(self) -> None:
+        """Wait for host copies left in flight by load_uvstress / export_uvFstress."""
+        A.check(self.lib.mpm_sync_transfers(), "mpm_sync_transfers")
+
     def export_grid(self, scene: int = 0):
         ng = self.scenes[scene].n_grid
         gm = torch.empty((ng, ng, ng), dtype=torch.float32, device=self.device)

@@ -203,9 +203,8 @@ class MPMSimulator:
     def load_uvstress_from_tensor(self, tensor_u, tensor_v, tensor_stress, clone=True,
                                   device="cuda:0"):
         """engine_stress/mpm_solver_warp.py:253-266 (the learned-stress hook)."""
-        self._engine.load(A.FIELD_U, tensor_u)
-        self._engine.load(A.FIELD_V, tensor_v)
-        self._engine.load(A.FIELD_STRESS, tensor_stress)
+        self._engine.load_uvstress(torch.as_tensor(tensor_u), torch.as_tensor(tensor_v),
+                                   torch.as_tensor(tensor_stress))
 
     # extensions (no reference counterpart)
     def load_vol_from_tensor(self, tensor_vol):
@@ -248,9 +247,9 @@ class MPMSimulator:
     def export_uvFstress_from_warp(self, device="cuda:0"):
         """engine_stress/mpm_solver_warp.py:305-310 -> (u, v, F_disp, stress)."""
         n = self.n_particles
-        e = self._engine
-        return (e.export(A.FIELD_U).reshape(n, 3), e.export(A.FIELD_V).reshape(n, 3),
-                self._f_disp(), e.export(A.FIELD_STRESS).reshape(n, 3, 3))
+        u, v, fd, st = self._engine.export_uvFstress()
+        fd = self._f_disp_loaded.clone() if self._f_disp_loaded is not None else fd.reshape(n, 3, 3)
+        return u.reshape(n, 3), v.reshape(n, 3), fd, st.reshape(n, 3, 3)
 
     # --------------------------------------------------------------- colliders
     def add_surface_collider(self, point, normal, surface="sticky", friction=0.0,
