@@ -42,7 +42,7 @@ constexpr int64_t kStateBytesPerParticle = mpm::kRecWords * 4 + 4;
 struct WsLayout {
     int64_t order, counts, cell_counts, cell_start, cell_cursor, tile_sums, ticket, chunks, n_chunks,
         blocks, n_blocks, grid_acc, grid_v, block_flag, active_list, n_active, n_active_prev, staging,
-        total;
+        slot_of_uid, total;
     int nbk, n_tiles;
 };
 
@@ -74,6 +74,7 @@ WsLayout ws_layout(const MpmPlan &p) {
     // host transfers: [u, v, stress in: 15 n][u, v, F_disp, stress out: 24 n] (disjoint, so the
     // next step's input copy may run while this step's output copy is in flight)
     L.staging = take(n * 39 * 4);
+    L.slot_of_uid = take(n * 4);
     L.total = o;
     return L;
 }
@@ -114,6 +115,7 @@ mpm::Ctx make_ctx(const MpmBuffers *b, void *stream, int which) {
     ws.n_active = reinterpret_cast<int *>(w + L.n_active);
     ws.n_active_prev = reinterpret_cast<int *>(w + L.n_active_prev);
     ws.staging = reinterpret_cast<float *>(w + L.staging);
+    ws.slot_of_uid = reinterpret_cast<int *>(w + L.slot_of_uid);
     ws.nbk = L.nbk;
     ws.n_tiles = L.n_tiles;
     ws.max_chunks = (int)p.max_chunks;

@@ -75,6 +75,7 @@ struct Ws {  // workspace
     int *n_active;
     int *n_active_prev;  // active blocks of the previous substep (to clear)
     float *staging;
+    int *slot_of_uid;  // user particle -> slot of the live state (host transfers)
     int nbk;          // buckets = total_blocks + 1 (last = out of domain)
     int n_tiles;
     int max_chunks;

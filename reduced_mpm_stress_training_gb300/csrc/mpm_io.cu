@@ -67,16 +67,27 @@ __global__ void export_kernel(PState st, int n, int field, int nc, float *__rest
     }
 }
 
-// load_uvstress_from_tensor (mpm_solver_warp.py:253-266) in one pass: u, v
-// and stress of each slot's user particle into its record (quads 2, 3, 5-7;
-// the C words sharing quads 3 and 5 are kept)
-__global__ void load_uvstress_kernel(PState st, int n, const float *__restrict__ u, const float *__restrict__ v,
-                                     const float *__restrict__ tau) {
+// slot_of_uid[uid] = slot for the live state: the two transfer kernels below
+// walk the particles in USER order, so their host-side arrays are read and
+// written coalesced and only the 160-byte records are gathered (whole
+// sectors) -- scattering 12- and 36-byte rows by uid instead leaves partial
+// sectors that L2 cannot merge once the arrays outgrow it
+__global__ void slot_of_uid_kernel(PState st, int n, int *__restrict__ inv) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int64_t id = __float_as_int(ldrec(st, i, 1).y);
+    inv[__float_as_int(ldrec(st, i, 1).y)] = i;
+}
+
+// load_uvstress_from_tensor (mpm_solver_warp.py:253-266) in one pass: u, v
+// and stress of user particle `id` into its record (quads 2, 3, 5-7; the C
+// words sharing quads 3 and 5 are kept)
+__global__ void load_uvstress_kernel(PState st, int n, const int *__restrict__ inv, const float *__restrict__ u,
+                                     const float *__restrict__ v, const float *__restrict__ tau) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const int i = inv[id];
     const float4 q3 = ldrec(st, i, 3), q5 = ldrec(st, i, 5);
-    const float *pu = u + id * 3, *pv = v + id * 3, *pt = tau + id * 9;
+    const float *pu = u + (int64_t)id * 3, *pv = v + (int64_t)id * 3, *pt = tau + (int64_t)id * 9;
     strec(st, i, 2, make_float4(pu[0], pu[1], pu[2], pv[0]));
     strec(st, i, 3, make_float4(pv[1], pv[2], q3.z, q3.w));
     strec(st, i, 5, make_float4(q5.x, q5.y, q5.z, pt[0]));
@@ -85,15 +96,16 @@ __global__ void load_uvstress_kernel(PState st, int n, const float *__restrict__
 }
 
 // export_uvFstress_from_warp (mpm_solver_warp.py:305-310) in one pass: u, v,
-// F - I (:16-19) and stress of each slot, written at its user index
-__global__ void export_uvFstress_kernel(PState st, int n, float *__restrict__ u, float *__restrict__ v,
-                                        float *__restrict__ fd, float *__restrict__ tau) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// F - I (:16-19) and stress of user particle `id`
+__global__ void export_uvFstress_kernel(PState st, int n, const int *__restrict__ inv, float *__restrict__ u,
+                                        float *__restrict__ v, float *__restrict__ fd, float *__restrict__ tau) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const int i = inv[id];
     const float4 q1 = ldrec(st, i, 1), q2 = ldrec(st, i, 2), q3 = ldrec(st, i, 3), q5 = ldrec(st, i, 5),
                  q6 = ldrec(st, i, 6), q7 = ldrec(st, i, 7), q8 = ldrec(st, i, 8), q9 = ldrec(st, i, 9);
-    const int64_t id = __float_as_int(q1.y);
-    float *pu = u + id * 3, *pv = v + id * 3, *pf = fd + id * 9, *pt = tau + id * 9;
+    float *pu = u + (int64_t)id * 3, *pv = v + (int64_t)id * 3, *pf = fd + (int64_t)id * 9,
+          *pt = tau + (int64_t)id * 9;
     pu[0] = q2.x; pu[1] = q2.y; pu[2] = q2.z;
     pv[0] = q2.w; pv[1] = q3.x; pv[2] = q3.y;
     pf[0] = q8.x - 1.0f; pf[1] = q8.y; pf[2] = q8.z; pf[3] = q8.w; pf[4] = q9.x - 1.0f;
@@ -187,13 +199,16 @@ cudaError_t launch_export(const Ctx &cx, int field, float *dst) {
 
 cudaError_t launch_load_uvstress(const Ctx &cx, const float *u, const float *v, const float *tau) {
     if (cx.n == 0) return cudaSuccess;
-    load_uvstress_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, u, v, tau);
+    slot_of_uid_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, cx.ws.slot_of_uid);
+    load_uvstress_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, cx.ws.slot_of_uid, u, v, tau);
     return cudaGetLastError();
 }
 
 cudaError_t launch_export_uvFstress(const Ctx &cx, float *u, float *v, float *fd, float *tau) {
     if (cx.n == 0) return cudaSuccess;
-    export_uvFstress_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, u, v, fd, tau);
+    slot_of_uid_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, cx.ws.slot_of_uid);
+    export_uvFstress_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, cx.ws.slot_of_uid, u, v,
+                                                                           fd, tau);
     return cudaGetLastError();
 }
 
