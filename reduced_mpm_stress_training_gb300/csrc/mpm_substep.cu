@@ -435,6 +435,18 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// three velocity components: x, y as a pair for the two-wide FP32 FMA, z alone
+struct V3 {
+    float2 xy;
+    float z;
+};
+__device__ __forceinline__ V3 v3zero() { return {make_float2(0.0f, 0.0f), 0.0f}; }
+__device__ __forceinline__ V3 v3of(const float4 &g) { return {make_float2(g.x, g.y), g.z}; }
+__device__ __forceinline__ V3 v3mul(float a, const V3 &x) { return {__fmul2_rn(make_float2(a, a), x.xy), a * x.z}; }
+__device__ __forceinline__ V3 v3fma(float a, const V3 &x, const V3 &acc) {
+    return {__ffma2_rn(make_float2(a, a), x.xy, acc.xy), fmaf(a, x.z, acc.z)};
+}
+
 constexpr int kG2PQuads = 5;  // record quads G2P reads: 0, 1, 2, 8, 9
 __device__ __forceinline__ int g2p_quad(int q) { return q < 3 ? q : q + 5; }
 
@@ -558,48 +570,42 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
                 //   nv  = sum_ijk wx_i wy_j wz_k g
                 //   nF  = sum g (x) (dwx wy wz, wx dwy wz, wx wy dwz)   (times inv_dx)
                 //   M_c = sum (w g) * (ijk)_c,  C = 4 inv_dx (M - nv (x) fx)
-                // z first (S, D, K per (i,j)), then y, then x.
-                float nv[3] = {0.f, 0.f, 0.f}, nF[9], M[9];
-#pragma unroll
-                for (int k = 0; k < 9; ++k) { nF[k] = 0.f; M[k] = 0.f; }
+                // z first (S, D, K per (i,j)), then y, then x.  Velocity
+                // components x, y ride together in Blackwell's two-wide FP32
+                // FMA (a V3 is (xy pair, z)); nF and M are kept by column.
+                V3 nvp = v3zero(), nF0 = v3zero(), nF1 = v3zero(), nF2 = v3zero();
+                V3 M0 = v3zero(), M1 = v3zero(), M2 = v3zero();
+                const float wz0 = W.w[2][0], wz1 = W.w[2][1], wz2 = W.w[2][2];
+                const float dz0 = W.dw[2][0], dz1 = W.dw[2][1], dz2 = W.dw[2][2];
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
-                    float Ti[3] = {0.f, 0.f, 0.f}, Ui[3] = {0.f, 0.f, 0.f}, Ri[3] = {0.f, 0.f, 0.f};
-                    float Ji[3] = {0.f, 0.f, 0.f}, Ki[3] = {0.f, 0.f, 0.f};
+                    V3 Ti = v3zero(), Ui = v3zero(), Ri = v3zero(), Ji = v3zero(), Ki = v3zero();
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
                         const float4 *row = tile + ((lx + i) * kTile + (ly + j)) * kTile + lz;
-                        const float4 g0 = row[0], g1 = row[1], g2 = row[2];
-                        const float gz[3][3] = {{g0.x, g0.y, g0.z}, {g1.x, g1.y, g1.z}, {g2.x, g2.y, g2.z}};
-                        float Sz[3], Dz[3], Kz[3];
-#pragma unroll
-                        for (int r = 0; r < 3; ++r) {
-                            Sz[r] = W.w[2][0] * gz[0][r] + W.w[2][1] * gz[1][r] + W.w[2][2] * gz[2][r];
-                            Dz[r] = W.dw[2][0] * gz[0][r] + W.dw[2][1] * gz[1][r] + W.dw[2][2] * gz[2][r];
-                            Kz[r] = W.w[2][1] * gz[1][r] + 2.0f * (W.w[2][2] * gz[2][r]);
-                        }
+                        const V3 g0 = v3of(row[0]), g1 = v3of(row[1]), g2 = v3of(row[2]);
+                        const V3 Sz = v3fma(wz2, g2, v3fma(wz1, g1, v3mul(wz0, g0)));
+                        const V3 Dz = v3fma(dz2, g2, v3fma(dz1, g1, v3mul(dz0, g0)));
+                        const V3 Kz = v3fma(2.0f * wz2, g2, v3mul(wz1, g1));
                         const float wy = W.w[1][j], dwy = W.dw[1][j];
-#pragma unroll
-                        for (int r = 0; r < 3; ++r) {
-                            Ti[r] += wy * Sz[r];
-                            Ui[r] += dwy * Sz[r];
-                            Ri[r] += wy * Dz[r];
-                            Ki[r] += wy * Kz[r];
-                            if (j > 0) Ji[r] += (float)j * (wy * Sz[r]);
-                        }
+                        Ti = v3fma(wy, Sz, Ti);
+                        Ui = v3fma(dwy, Sz, Ui);
+                        Ri = v3fma(wy, Dz, Ri);
+                        Ki = v3fma(wy, Kz, Ki);
+                        if (j > 0) Ji = v3fma((float)j * wy, Sz, Ji);
                     }
                     const float wx = W.w[0][i], dwx = W.dw[0][i];
-#pragma unroll
-                    for (int r = 0; r < 3; ++r) {
-                        nv[r] += wx * Ti[r];
-                        nF[r * 3 + 0] += dwx * Ti[r];
-                        nF[r * 3 + 1] += wx * Ui[r];
-                        nF[r * 3 + 2] += wx * Ri[r];
-                        if (i > 0) M[r * 3 + 0] += (float)i * (wx * Ti[r]);
-                        M[r * 3 + 1] += wx * Ji[r];
-                        M[r * 3 + 2] += wx * Ki[r];
-                    }
+                    nvp = v3fma(wx, Ti, nvp);
+                    nF0 = v3fma(dwx, Ti, nF0);
+                    nF1 = v3fma(wx, Ui, nF1);
+                    nF2 = v3fma(wx, Ri, nF2);
+                    if (i > 0) M0 = v3fma((float)i * wx, Ti, M0);
+                    M1 = v3fma(wx, Ji, M1);
+                    M2 = v3fma(wx, Ki, M2);
                 }
+                const float nv[3] = {nvp.xy.x, nvp.xy.y, nvp.z};
+                float nF[9] = {nF0.xy.x, nF1.xy.x, nF2.xy.x, nF0.xy.y, nF1.xy.y, nF2.xy.y, nF0.z, nF1.z, nF2.z};
+                const float M[9] = {M0.xy.x, M1.xy.x, M2.xy.x, M0.xy.y, M1.xy.y, M2.xy.y, M0.z, M1.z, M2.z};
                 float nC[9];
                 const float c4 = 4.0f * inv_dx;
 #pragma unroll
