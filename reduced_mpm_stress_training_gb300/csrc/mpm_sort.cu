@@ -148,8 +148,8 @@ __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__rest
         int b = b0 + j;
         if (b >= ws.nbk) break;
         ws.counts[b] = 0;
-        // the out-of-domain bucket always gets its cursor: its particles are
-        // not re-counted by G2P, and they sort after every counted particle
+        // the out-of-domain bucket always gets its cursor (its particles sort
+        // after every other one; G2P's copy chunks count them again)
         if (cnt[j] > 0 || b == ws.nbk - 1) {
             // cell offsets inside the block; zero its cell histogram
             int4 *cc = reinterpret_cast<int4 *>(ws.cell_counts + (int64_t)b * 64);

@@ -532,7 +532,8 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
             if (mine) {
 #pragma unroll
                 for (int q = 0; q < kRecQuads; ++q) strec(out, pos, q, ldrec(st, slot, q));
-                out.key[pos] = st.key[slot];
+                key = st.key[slot];  // counted again below: the next sort keeps their copy chunk
+                out.key[pos] = key;
             }
         } else if (mine) {
             const MpmScene &S = scenes[ch.w];

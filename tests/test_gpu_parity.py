@@ -394,3 +394,32 @@ def test_fused_uvstress_transfers_match_per_field(cuda):
     # the simulator's reference-named methods go through the same calls
     su, sv, sfd, sst = sim.export_uvFstress_from_warp()
     assert torch.equal(su.reshape(-1), uu) and torch.equal(sst.reshape(-1), ss)
+
+
+def test_particle_leaving_the_domain_is_carried_over(cuda):
+    """A particle that flies out of the grid is frozen there (skipped by P2G
+    and G2P, flagged out-of-domain) and its record is carried over by every
+    later substep's re-sort, while the others keep matching the oracle."""
+    sc = S.small_column(1024, 32)
+    x0, v0, vol, mass = sc.particles()
+    x0[5] = (0.94, 0.5, 0.5)   # stencil base 29 = n - 3: the last valid cell
+    v0[5] = (5.0, 0.0, 0.0)    # leaves after ~26 substeps (dx / dt = 312.5 m/s)
+    sim = gpu_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass, colliders=False)
+    sim.on_error = "ignore"
+    ref = oracle_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass, colliders=False)
+    ref64 = oracle_sim(sc, bits=64, x0=x0, v0=v0, vol=vol, mass=mass, colliders=False)
+    bits = 0
+    for k in range(40):
+        sim.p2g2p(k, sc.dt)
+        bits |= sim._engine.status()
+        sim._engine.clear_status()
+        ref.p2g2p(sc.dt)
+        ref64.p2g2p(sc.dt)
+    assert bits & A.ST_OUT_OF_DOMAIN
+    assert not bits & A.ST_INTERNAL, bits
+    errs = compare(sim, ref, fields=("x", "v", "F"))
+    tol = _step_tol(ref, ref64, errs)
+    assert all(errs[f] < tol[f] for f in errs), (errs, tol)
+    g = gpu_state(sim)
+    assert g["x"][5, 0] * 32 - 0.5 >= 30  # outside, where it stopped
+    assert abs(g["x"][5, 0] - float((ref.x0 + ref.u)[5, 0])) < 1e-6
