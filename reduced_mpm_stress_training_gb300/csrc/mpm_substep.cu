@@ -56,7 +56,7 @@ namespace mpm {
 // lanes of a quarter-warp (one 128-bit shared access phase) holding two
 // y-adjacent rows of 4 cells hit 8 distinct bank groups for every offset.
 // ---------------------------------------------------------------------------
-constexpr int kP2GWarps = 4;
+constexpr int kP2GWarps = 1;  // one warp per CTA: the hardware balances unequal blocks
 constexpr int kRunMax = 4;     // most particles of one cell a lane takes per round
 constexpr int kP2GQuads = 8;   // record quads P2G reads (q0-q7, 128 B)
 constexpr int kRowSlots = 8;
@@ -719,11 +719,11 @@ cudaError_t launch_p2g(const Ctx &cx, float dt) {
         if (e != cudaSuccess) return e;
         if (dev >= 0 && dev < 64) attr_set[dev] = true;
     }
-    // up to eight CTAs (32 warps) per SM, several times the resident ones:
-    // the rest start as others finish, which balances blocks of unequal size;
+    // up to 32 single-warp CTAs per SM, several times the resident ones: the
+    // rest start as others finish, which balances blocks of unequal size;
     // warps loop over blocks when there are more blocks than warps
     int64_t want = (cx.total_blocks + kP2GWarps - 1) / kP2GWarps;
-    int grid = (int)(want < (int64_t)cx.num_sms * 8 ? want : (int64_t)cx.num_sms * 8);
+    int grid = (int)(want < (int64_t)cx.num_sms * 32 ? want : (int64_t)cx.num_sms * 32);
     if (grid < 1) grid = 1;
     p2g_kernel<<<grid, kP2GWarps * 32, bytes, cx.stream>>>(cx.scenes, cx.st, cx.ws, dt, cx.status);
     return cudaGetLastError();
