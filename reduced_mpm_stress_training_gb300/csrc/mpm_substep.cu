@@ -196,8 +196,8 @@ __device__ __forceinline__ void p2g_cp_async16(void *smem, const void *gmem) {
 }
 
 // queue the copy of one record (slot >= 0) into the lane's buffer b
-__device__ __forceinline__ void p2g_prefetch(P2GWarpSmem &sm, const PState &st, int slot, int b, int lane) {
-    if (slot >= 0) {
+__device__ __forceinline__ void p2g_prefetch(P2GWarpSmem &sm, const PState &st, int slot, int b, int lane, int n) {
+    if (slot >= 0 && slot < n) {
         const float4 *src = st.rec + (int64_t)slot * kRecQuads;
 #pragma unroll
         for (int q = 0; q < kP2GQuads; ++q) p2g_cp_async16(&sm.rec[b][q][lane], src + q);
@@ -255,7 +255,7 @@ __device__ __forceinline__ bool p2g_next_round(int &rem0, int &rem1, int &pos0, 
 }
 
 __global__ void __launch_bounds__(kP2GWarps * 32, 2) p2g_kernel(const MpmScene *__restrict__ scenes,
-                                                                PState st, Ws ws, float dt,
+                                                                int n_scenes, PState st, Ws ws, float dt,
                                                                 int *status) {
     extern __shared__ __align__(16) unsigned char p2g_smem_raw[];
     P2GWarpSmem *smem = reinterpret_cast<P2GWarpSmem *>(p2g_smem_raw);
@@ -267,6 +267,11 @@ __global__ void __launch_bounds__(kP2GWarps * 32, 2) p2g_kernel(const MpmScene *
     for (int bi = blockIdx.x * kP2GWarps + (int)(threadIdx.x >> 5); bi < nblk;
          bi += gridDim.x * kP2GWarps) {
         const int4 be = ws.blocks[bi];
+        if ((unsigned)be.x >= (unsigned)(ws.nbk - 1) || (unsigned)be.w >= (unsigned)n_scenes) {
+            // a damaged work list: skip, never index with it
+            if (lane == 0) atomicOr(status, MPM_ST_INTERNAL);
+            continue;
+        }
         const MpmScene &S = scenes[be.w];
         int bx, by, bz;
         chunk_block(S, be.x, bx, by, bz);
@@ -284,16 +289,17 @@ __global__ void __launch_bounds__(kP2GWarps * 32, 2) p2g_kernel(const MpmScene *
         bool haveA = p2g_next_round(rem0, rem1, pos0, pos1, lane, lt, sm.seg, startA, cellA, lenA, LA);
         int slA[kRunMax];
 #pragma unroll
-        for (int t = 0; t < kRunMax; ++t) slA[t] = t < lenA ? ws.order[startA + t] : -1;  // positions < n
+        for (int t = 0; t < kRunMax; ++t) slA[t] = t < lenA && startA + t < ws.n ? ws.order[startA + t] : -1;
         int buf = 0;
-        if (haveA) p2g_prefetch(sm, st, slA[0], 0, lane);
+        if (haveA) p2g_prefetch(sm, st, slA[0], 0, lane, ws.n);
         bool bad = false;
         while (haveA) {
             int startB, cellB, lenB, LB;
             const bool haveB = p2g_next_round(rem0, rem1, pos0, pos1, lane, lt, sm.seg, startB, cellB, lenB, LB);
             int slB[kRunMax];
 #pragma unroll
-            for (int t = 0; t < kRunMax; ++t) slB[t] = haveB && t < lenB ? ws.order[startB + t] : -1;
+            for (int t = 0; t < kRunMax; ++t)
+                slB[t] = haveB && t < lenB && startB + t < ws.n ? ws.order[startB + t] : -1;
             const int cx = cellA >> 4, cy = (cellA >> 2) & 3, cz = cellA & 3;
             float2 axy[27], azw[27];
 #pragma unroll
@@ -310,9 +316,11 @@ __global__ void __launch_bounds__(kP2GWarps * 32, 2) p2g_kernel(const MpmScene *
 #pragma unroll
                     for (int u = 0; u + 1 < kRunMax; ++u)
                         if (u == t && t + 1 < LA) nxt = slA[u + 1];
-                    p2g_prefetch(sm, st, nxt, buf ^ 1, lane);
+                    p2g_prefetch(sm, st, nxt, buf ^ 1, lane, ws.n);
                     asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-                    if (t < lenA) {
+                    if (t < lenA && slA[t] < 0) {
+                        bad = true;  // position or slot out of range: nothing was staged
+                    } else if (t < lenA) {
                         float4 q[kP2GQuads];
 #pragma unroll
                         for (int qq = 0; qq < kP2GQuads; ++qq) q[qq] = sm.rec[buf][qq][lane];
@@ -725,7 +733,8 @@ cudaError_t launch_p2g(const Ctx &cx, float dt) {
     int64_t want = (cx.total_blocks + kP2GWarps - 1) / kP2GWarps;
     int grid = (int)(want < (int64_t)cx.num_sms * 32 ? want : (int64_t)cx.num_sms * 32);
     if (grid < 1) grid = 1;
-    p2g_kernel<<<grid, kP2GWarps * 32, bytes, cx.stream>>>(cx.scenes, cx.st, cx.ws, dt, cx.status);
+    p2g_kernel<<<grid, kP2GWarps * 32, bytes, cx.stream>>>(cx.scenes, cx.n_scenes, cx.st, cx.ws, dt,
+                                                           cx.status);
     return cudaGetLastError();
 }
 
