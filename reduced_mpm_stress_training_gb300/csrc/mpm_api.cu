@@ -71,13 +71,21 @@ WsLayout ws_layout(const MpmPlan &p) {
     L.active_list = take(p.total_blocks * 4);
     L.n_active = take(4);
     L.n_active_prev = take(4);
-    // host transfers: [u, v, stress in: 15 n][u, v, F_disp, stress out: 24 n] (disjoint, so the
-    // next step's input copy may run while this step's output copy is in flight)
-    L.staging = take(n * 39 * 4);
+    // host transfers: [u, v, stress in: 15 n][u, v, F_disp, stress out: 2 x 24 n] (disjoint, so
+    // the next step's input copy and export may run while this step's output copy is in flight)
+    L.staging = take(n * 63 * 4);
     L.slot_of_uid = take(n * 4);
     L.total = o;
     return L;
 }
+
+}  // namespace
+
+// bytes at the start of the workspace that a substep touches: everything
+// but the host-transfer staging and the slot-of-uid table, which come last
+int64_t mpm::substep_workspace_bytes(const MpmPlan &p) { return ws_layout(p).staging; }
+
+namespace {
 
 mpm::PState state_view(void *base, int64_t stride) {
     mpm::PState s;
@@ -254,14 +262,17 @@ int mpm_export(MpmBuffers *b, int32_t field, float *dst, int32_t dst_on_host, vo
 // Side streams per device for the host copies of mpm_load_uvstress (input
 // lane) and mpm_export_uvFstress (output lane), and the events that order
 // them against the caller's stream.  An input copy waits only until the
-// previous load kernel has consumed the input staging; an output copy waits
-// for its export kernel, and the next export kernel waits for it to have
-// drained the output staging.  So the input copy of one step, the output copy
-// of the step before and the substep itself can all run at once.
+// previous load kernel has consumed the input staging.  Exports alternate
+// between two output staging halves: an output copy waits for its export
+// kernel, and an export kernel waits only for the copy that last drained
+// its half (two exports back).  So the input copy of one step, the output
+// copy of the step before and the substep itself can all run at once, and
+// the output copies run back to back.
 namespace {
 struct CopyLane {
     cudaStream_t stream = nullptr;
-    cudaEvent_t ready = nullptr, done = nullptr;
+    cudaEvent_t ready = nullptr, done[2] = {nullptr, nullptr};
+    int parity = 0;
 };
 CopyLane g_in[64], g_out[64];
 
@@ -274,7 +285,8 @@ cudaError_t lane_of(CopyLane *lanes, CopyLane *&lane) {
     if (!L.stream) {
         if ((e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking)) != cudaSuccess) return e;
         if ((e = cudaEventCreateWithFlags(&L.ready, cudaEventDisableTiming)) != cudaSuccess) return e;
-        if ((e = cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming)) != cudaSuccess) return e;
+        for (cudaEvent_t &d : L.done)
+            if ((e = cudaEventCreateWithFlags(&d, cudaEventDisableTiming)) != cudaSuccess) return e;
     }
     lane = &L;
     return cudaSuccess;
@@ -303,14 +315,14 @@ int mpm_load_uvstress(MpmBuffers *b, const float *u, const float *v, const float
     float *s = cx.ws.staging;  // input region: u, v, stress
     CopyLane *L = nullptr;
     MPM_CHECK(lane_of(g_in, L));
-    MPM_CHECK(cudaStreamWaitEvent(L->stream, L->done, 0));  // no-op before the first load
+    MPM_CHECK(cudaStreamWaitEvent(L->stream, L->done[0], 0));  // no-op before the first load
     MPM_CHECK(cudaMemcpyAsync(s, u, n * 12, cudaMemcpyHostToDevice, L->stream));
     MPM_CHECK(cudaMemcpyAsync(s + 3 * n, v, n * 12, cudaMemcpyHostToDevice, L->stream));
     MPM_CHECK(cudaMemcpyAsync(s + 6 * n, stress, n * 36, cudaMemcpyHostToDevice, L->stream));
     MPM_CHECK(cudaEventRecord(L->ready, L->stream));
     MPM_CHECK(cudaStreamWaitEvent(cx.stream, L->ready, 0));
     MPM_CHECK(mpm::launch_load_uvstress(cx, s, s + 3 * n, s + 6 * n));
-    MPM_CHECK(cudaEventRecord(L->done, cx.stream));  // input staging consumed
+    MPM_CHECK(cudaEventRecord(L->done[0], cx.stream));  // input staging consumed
     b->keys_valid = 0;
     return MPM_OK;
 }
@@ -321,14 +333,16 @@ int mpm_export_uvFstress(MpmBuffers *b, float *u, float *v, float *F_disp, float
     mpm::Ctx cx = make_ctx(b, stream, b->cur);
     if (cx.n == 0) return MPM_OK;
     const size_t n = (size_t)cx.n;
-    float *s = cx.ws.staging + 15 * n;  // output region: u, v, F_disp, stress
     if (!dst_on_host) {
         MPM_CHECK(mpm::launch_export_uvFstress(cx, u, v, F_disp, stress));
         return MPM_OK;
     }
     CopyLane *L = nullptr;
     MPM_CHECK(lane_of(g_out, L));
-    MPM_CHECK(cudaStreamWaitEvent(cx.stream, L->done, 0));  // previous output copy drained the staging
+    const int h = L->parity;
+    L->parity ^= 1;
+    float *s = cx.ws.staging + 15 * n + (size_t)h * 24 * n;  // output half h: u, v, F_disp, stress
+    MPM_CHECK(cudaStreamWaitEvent(cx.stream, L->done[h], 0));  // the copy that last used half h drained it
     MPM_CHECK(mpm::launch_export_uvFstress(cx, s, s + 3 * n, s + 6 * n, s + 15 * n));
     MPM_CHECK(cudaEventRecord(L->ready, cx.stream));
     MPM_CHECK(cudaStreamWaitEvent(L->stream, L->ready, 0));
@@ -336,8 +350,8 @@ int mpm_export_uvFstress(MpmBuffers *b, float *u, float *v, float *F_disp, float
     MPM_CHECK(cudaMemcpyAsync(v, s + 3 * n, n * 12, cudaMemcpyDeviceToHost, L->stream));
     MPM_CHECK(cudaMemcpyAsync(F_disp, s + 6 * n, n * 36, cudaMemcpyDeviceToHost, L->stream));
     MPM_CHECK(cudaMemcpyAsync(stress, s + 15 * n, n * 36, cudaMemcpyDeviceToHost, L->stream));
-    MPM_CHECK(cudaEventRecord(L->done, L->stream));
-    if (dst_on_host == 1) MPM_CHECK(cudaEventSynchronize(L->done));
+    MPM_CHECK(cudaEventRecord(L->done[h], L->stream));
+    if (dst_on_host == 1) MPM_CHECK(cudaEventSynchronize(L->done[h]));
     return MPM_OK;
 }
 

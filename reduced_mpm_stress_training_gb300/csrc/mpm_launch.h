@@ -46,6 +46,7 @@ cudaError_t launch_return_map_vjp(const MpmScene &scene, const float *Ft, const 
                                   float *Ftb, double *thb, int64_t n, cudaStream_t st);
 // saved grids for the reverse pass (mpm_checkpoint.cu)
 int64_t substep_grid_bytes(int64_t total_blocks, int64_t n, int64_t max_chunks);
+int64_t substep_workspace_bytes(const MpmPlan &p);  // the substep's prefix of the workspace
 cudaError_t launch_save_grid(const Ctx &cx, void *dst);
 cudaError_t launch_load_grid(const Ctx &cx, const void *src);
 cudaError_t launch_clear_grid(const Ctx &cx);

@@ -13,9 +13,12 @@
 //
 // Limits and behaviour:
 //   * The array is kNoAllocWorkspaceBytes (16 MiB) and every GPU that loads
-//     the library holds it until the process exits.  Plans whose
-//     workspace_bytes exceed it are rejected with MPM_ERR_SIZE (16 MiB covers
-//     e.g. a 64^3 grid with 32,768 particles).
+//     the library holds it until the process exits.  It holds the part of
+//     the workspace a substep uses (all but the host-transfer staging, which
+//     this entry point never touches); plans whose substep part exceeds it
+//     are rejected with MPM_ERR_SIZE (16 MiB covers a 64^3 grid -- about
+//     11 MiB of grid and cell arrays -- with up to about a million
+//     particles at 4-5 bytes each; a 128^3 grid does not fit).
 //   * All calls share the array, and it keeps the last call's contents.  Each
 //     call therefore clears the part it uses and recomputes the sort keys
 //     from the particle positions (a full re-sort every call), so calls from
@@ -65,15 +68,14 @@ void *noalloc_workspace(int *err) {
 
 extern "C" int mpm_p2g2p_noalloc(MpmBuffers *b, float time, float dt, void *stream) {
     if (!b || !b->state[0] || !b->state[1] || !b->scenes || !b->status) return MPM_ERR_ARG;
-    if (b->plan.workspace_bytes < 0 || (size_t)b->plan.workspace_bytes > kNoAllocWorkspaceBytes)
-        return MPM_ERR_SIZE;
+    const int64_t need = mpm::substep_workspace_bytes(b->plan);
+    if (need < 0 || (size_t)need > kNoAllocWorkspaceBytes) return MPM_ERR_SIZE;
     int err = MPM_OK;
     void *ws = noalloc_workspace(&err);
     if (!ws) return err;
     // the array holds whatever the last call left: start from a cleared
     // workspace and keys recomputed from the positions
-    cudaError_t e = cudaMemsetAsync(ws, 0, (size_t)b->plan.workspace_bytes,
-                                    static_cast<cudaStream_t>(stream));
+    cudaError_t e = cudaMemsetAsync(ws, 0, (size_t)need, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return MPM_ERR_CUDA;
     MpmBuffers local = *b;
     local.workspace = ws;
