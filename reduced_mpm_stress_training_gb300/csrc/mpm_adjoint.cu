@@ -319,7 +319,13 @@ __global__ void __launch_bounds__(128) g2p_adjoint_kernel(const MpmScene *__rest
     float thb[3] = {0.0f, 0.0f, 0.0f};
     for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < ws.n; pos += gridDim.x * blockDim.x) {
         const int slot = ws.order[pos];
-        const float *w = recw(st, slot);
+        // the record quads this kernel reads (x0 | uid, F8 | u | F0-7), as
+        // 16-byte loads; w indexes them by record word
+        float4 rq[kRecQuads];
+#pragma unroll
+        for (int q = 0; q < kRecQuads; ++q)
+            rq[q] = (q < 3 || q >= 8) ? ldrec(st, slot, q) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float *w = reinterpret_cast<const float *>(rq);
         const int uid = __float_as_int(w[rec::UID]);
         const MpmScene &S = scenes[scene_of_particle(scenes, n_scenes, uid)];
         PData p;
@@ -515,7 +521,11 @@ __global__ void __launch_bounds__(128) p2g_adjoint_kernel(const MpmScene *__rest
                                                           float *__restrict__ adj_in, float dt) {
     for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < ws.n; pos += gridDim.x * blockDim.x) {
         const int slot = ws.order[pos];
-        const float *w = recw(st, slot);
+        // record quads 0-7 (x0, m | vol, uid | u, v | C | tau) as 16-byte loads
+        float4 rq[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) rq[q] = ldrec(st, slot, q);
+        const float *w = reinterpret_cast<const float *>(rq);
         const int uid = __float_as_int(w[rec::UID]);
         const MpmScene &S = scenes[scene_of_particle(scenes, n_scenes, uid)];
         PData p;
