@@ -423,3 +423,36 @@ def test_particle_leaving_the_domain_is_carried_over(cuda):
     g = gpu_state(sim)
     assert g["x"][5, 0] * 32 - 0.5 >= 30  # outside, where it stopped
     assert abs(g["x"][5, 0] - float((ref.x0 + ref.u)[5, 0])) < 1e-6
+
+
+def test_tilted_timed_colliders_match_oracle(cuda):
+    """A tilted slip plane (normal not along an axis, friction given) that is
+    active only for substeps 3-7, plus the bounding box from substep 2 on:
+    every node below the plane is zeroed while it is active (the reference
+    zeroes for all surface types, engine_stress/mpm_solver_warp.py:449), and
+    the windows switch on the same substeps as the oracle's."""
+    sc = S.small_column(8192, 32)
+    dt = sc.dt
+    x0, v0, vol, mass = sc.particles()
+    plane = dict(point=(0.5, 0.5, 0.32), normal=(0.3, -0.2, 1.0), surface="slip", friction=0.1,
+                 start_time=2.5 * dt, end_time=6.5 * dt)
+    box = dict(start_time=1.5 * dt, end_time=999.0)
+    sim = gpu_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass, colliders=False)
+    sim.add_surface_collider(**plane)
+    sim.add_bounding_box(**box)
+    m = O.make_model(sc.n_grid, sc.grid_lim, material=sc.material, E=sc.E, nu=sc.nu,
+                     friction_angle=sc.friction_angle, gravity=sc.gravity)
+    cols = [O.surface_collider(**plane), O.bounding_box(**box)]
+    ref = O.OracleSim(m, x0, mass, vol, v0, bits=32, colliders=cols)
+    ref64 = O.OracleSim(m, x0, mass, vol, v0, bits=64, colliders=cols)
+    moved = []
+    for k in range(10):
+        sim.p2g2p(k, dt)
+        ref.p2g2p(dt)
+        ref64.p2g2p(dt)
+        errs = compare(sim, ref, fields=("x", "v", "F"))
+        tol = _step_tol(ref, ref64, errs)
+        assert all(errs[f] < tol[f] for f in errs), (k, errs, tol)
+        moved.append(float(np.abs(gpu_state(sim)["v"]).max()))
+    assert sim.check_status() == 0
+    assert max(moved) > 0.0
