@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 1
+#define MPM_ABI_VERSION 2
 #define MPM_MAX_COLLIDERS 8
 
 /* return codes */
@@ -48,22 +48,40 @@ extern "C" {
 #define MPM_SAND 2
 
 /* collider kinds */
-#define MPM_COLLIDER_SURFACE 0 /* add_surface_collider, mpm_solver_warp.py:407-451 */
-#define MPM_COLLIDER_BOX 1     /* add_bounding_box,     mpm_solver_warp.py:499-525 */
+#define MPM_COLLIDER_SURFACE 0 /* add_surface_collider(2), mpm_solver_warp.py:407-497      */
+#define MPM_COLLIDER_BOX 1     /* add_bounding_box,           mpm_solver_warp.py:499-525    */
+#define MPM_COLLIDER_VPLANE 2  /* set_velocity_on_infinite_plane, mpm_solver_warp.py:527-568 */
+#define MPM_COLLIDER_CIRCLE 3  /* set_column_moving_as_circle,    mpm_solver_warp.py:570-607 */
+#define MPM_COLLIDER_DISK 4    /* set_rotation_on_disk,           mpm_solver_warp.py:609-665 */
+#define MPM_COLLIDER_CUBE 5    /* set_velocity_on_cube,           mpm_solver_warp.py:667-695 */
+#define MPM_COLLIDER_SPHERE 6  /* add_sphere_leader,              mpm_solver_warp.py:697-720 */
 
-/* Dirichlet_collider subset used by the two grid boundary kernels
- * (engine_stress/warp_utils.py:126-151).  normal must be unit length. */
+/* Dirichlet_collider (engine_stress/warp_utils.py:126-151).  normal, x_unit
+ * and y_unit must be unit length.  A collider is active while
+ * start_time <= time < end_time; the moving kinds (VPLANE, CIRCLE, CUBE,
+ * SPHERE) advance `point` on the device after each active substep's grid
+ * update, as the reference's modify_bc callbacks do on the host. */
 typedef struct MpmCollider {
     int32_t kind;         /* MPM_COLLIDER_*                                      */
-    int32_t surface_type; /* 0 sticky, 1 slip, 2 separate; all three zero the
-                             node velocity, as the reference does (:449)         */
+    int32_t surface_type; /* SURFACE: 0 sticky, 1 slip, 2 separate; all three
+                             zero the node velocity, as the reference does (:449) */
     float point[3];
     float normal[3];
     float friction;
     float start_time; /* active while start_time <= time < end_time */
     float end_time;
+    int32_t reset;        /* VPLANE, DISK, CUBE: zero velocities shortly after end_time */
+    float velocity[3];    /* VPLANE, CUBE, SPHERE: velocity given to the covered nodes */
+    float threshold;      /* VPLANE: half-thickness of the slab |(x - point).normal|  */
+    float radius;         /* CIRCLE, DISK, SPHERE                                */
+    float width;          /* DISK: half-thickness; CUBE: half-width               */
+    float height;         /* CIRCLE: half-height of the column                    */
+    float v_scale;        /* CIRCLE: speed; DISK: angular speed                   */
+    float x_unit[3];      /* DISK: in-plane axes                                  */
+    float y_unit[3];
+    float R;              /* CIRCLE: orbit radius                                 */
     float pad0;
-} MpmCollider; /* 48 bytes */
+} MpmCollider; /* 112 bytes */
 
 /* One scene: MPMModelStruct (engine_stress/warp_utils.py:61-81) plus its
  * particle range and grid-block range.  A plain simulator is one scene; the
@@ -84,7 +102,7 @@ typedef struct MpmScene {
     int64_t particle_count;
     int64_t block_begin;    /* (plan) first global 4x4x4 grid-block id        */
     MpmCollider colliders[MPM_MAX_COLLIDERS];
-} MpmScene; /* 464 bytes */
+} MpmScene; /* 976 bytes */
 
 /* Sizes computed by mpm_plan. */
 typedef struct MpmPlan {
@@ -110,10 +128,14 @@ typedef struct MpmBuffers {
                                 flips it (G2P writes the updated records, sorted
                                 by cell, into the other buffer)                 */
     int32_t keys_valid;      /* 0 after a load that moves particles             */
-    int32_t reserved0;
+    int32_t collider_flags;  /* (set by mpm_upload_scenes) MPM_CF_* of the table */
     int32_t pad0;
     int64_t substep;         /* substeps taken since mpm_init                   */
 } MpmBuffers;
+
+/* collider_flags bits */
+#define MPM_CF_EXTENDED 1 /* a collider of kind VPLANE..SPHERE (no adjoint for those) */
+#define MPM_CF_MOVING 2   /* a moving collider: mpm_grid_update advances its point  */
 
 /* State fields for mpm_load / mpm_export.  Layout on the caller side is the
  * reference's: AoS, user particle order, vec3 = 3 floats, mat33 = 9 floats

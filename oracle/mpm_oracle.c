@@ -94,7 +94,11 @@ typedef struct {
     double gravity[3]; /* reference: (0, -g, 0), mpm_utils.py:236 */
 } OrcModel;
 
-/* kind 0 = surface collider, 1 = bounding box (mpm_solver_warp.py:407,499). */
+/* Dirichlet_collider (warp_utils.py:126-151).  kind 0 = surface collider,
+ * 1 = bounding box, 2 = velocity on an infinite plane, 3 = column moving as
+ * a circle, 4 = rotation on a disk, 5 = velocity on a cube, 6 = sphere
+ * leader (mpm_solver_warp.py:407-720).  The moving kinds' points are
+ * advanced by the caller between substeps (the reference's modify_bc). */
 typedef struct {
     int32_t kind;
     int32_t surface_type;
@@ -102,6 +106,12 @@ typedef struct {
     double normal[3];
     double friction;
     double start_time, end_time;
+    int32_t reset;
+    int32_t pad;
+    double velocity[3];
+    double threshold, radius, width, height, v_scale;
+    double x_unit[3], y_unit[3];
+    double R;
 } OrcCollider;
 
 /* ------------------------------------------------------------------ */
@@ -609,6 +619,103 @@ void PFX(collide_bounding_box)(const OrcModel *m, const OrcCollider *col, double
             }
 }
 
+/* float32 window tests, as the reference's kernels see float time and times */
+static int col_active(const OrcCollider *col, double time) {
+    return (float)time >= (float)col->start_time && (float)time < (float)col->end_time;
+}
+
+/* angle of the circling column's bottom point about (0.5, *, 0.5)
+ * (mpm_solver_warp.py:585-592), float32 */
+static float circle_theta(const OrcCollider *col) {
+    const float z0 = (float)col->point[0] - 0.5f, z1 = (float)col->point[1], z2 = (float)col->point[2] - 0.5f;
+    const float len = sqrtf(z0 * z0 + z1 * z1 + z2 * z2);
+    float c = z0 / len;
+    c = c < -1.0f ? -1.0f : (c > 1.0f ? 1.0f : c);
+    const float th = acosf(c);
+    return z2 < 0.0f ? -th : th;
+}
+
+/* kinds 2-6: mpm_solver_warp.py:545-559, :580-592, :635-659, :680-689,
+ * :709-714; every node of the dense grid, as the reference launches them */
+void PFX(collide_extended)(const OrcModel *m, const OrcCollider *col, double time, real dt, real *gvout) {
+    const int act = col_active(col, time);
+    const float tf = (float)time, dtf = (float)dt;
+    const int n = m->n_grid;
+    const float dx = (float)m->dx;
+    const float pt[3] = {(float)col->point[0], (float)col->point[1], (float)col->point[2]};
+    const float nr[3] = {(float)col->normal[0], (float)col->normal[1], (float)col->normal[2]};
+    const float vel[3] = {(float)col->velocity[0], (float)col->velocity[1], (float)col->velocity[2]};
+    const float xu[3] = {(float)col->x_unit[0], (float)col->x_unit[1], (float)col->x_unit[2]};
+    const float yu[3] = {(float)col->y_unit[0], (float)col->y_unit[1], (float)col->y_unit[2]};
+    const float thr = (float)col->threshold, rad = (float)col->radius, wid = (float)col->width;
+    const float hei = (float)col->height, vs = (float)col->v_scale, endf = (float)col->end_time;
+    const int reset_plane = !act && col->reset == 1 && tf < endf + 1.5f * dtf * 10.0f;
+    const int reset_all = !act && col->reset == 1 && tf < endf + 1.5f * dtf;
+    if (!act && !reset_plane && !reset_all) return;
+    const float cth = col->kind == 3 ? circle_theta(col) : 0.0f;
+#pragma omp parallel for schedule(static)
+    for (int ix = 0; ix < n; ++ix)
+        for (int iy = 0; iy < n; ++iy)
+            for (int iz = 0; iz < n; ++iz) {
+                real *vv = gvout + 3 * gidx(n, ix, iy, iz);
+                const float o0 = (float)ix * dx - pt[0], o1 = (float)iy * dx - pt[1], o2 = (float)iz * dx - pt[2];
+                float set[3];
+                int write = 0;
+                if (col->kind == 2) {
+                    const float dp = o0 * nr[0] + o1 * nr[1] + o2 * nr[2];
+                    if (fabsf(dp) <= thr) {
+                        write = act || reset_plane;
+                        for (int c = 0; c < 3; ++c) set[c] = act ? vel[c] : 0.0f;
+                    }
+                } else if (col->kind == 3) {
+                    if (act && o0 * o0 + o2 * o2 < rad * rad && fabsf(o1) < hei) {
+                        write = 1;
+                        set[0] = -vs * sinf(cth);
+                        set[1] = 0.0f;
+                        set[2] = vs * cosf(cth);
+                    }
+                } else if (col->kind == 4) {
+                    if (act) {
+                        const float dp = o0 * nr[0] + o1 * nr[1] + o2 * nr[2];
+                        const float rl = sqrtf(o1 * o1 + o2 * o2);
+                        if (fabsf(dp) < wid && rl < rad) {
+                            write = 1;
+                            if (rl > 0.0f) {  /* the reference divides 0 by 0 on the axis */
+                                float c = (o1 * xu[1] + o2 * xu[2]) / rl;
+                                c = c < -1.0f ? -1.0f : (c > 1.0f ? 1.0f : c);
+                                float th = acosf(c);
+                                if (o1 * yu[1] + o2 * yu[2] < 0.0f) th = -th;
+                                const float sx = -rl * sinf(th) * vs, sy = rl * cosf(th) * vs;
+                                for (int c2 = 0; c2 < 3; ++c2) set[c2] = sx * xu[c2] + sy * yu[c2];
+                            } else {
+                                set[0] = set[1] = set[2] = 0.0f;
+                            }
+                        }
+                    } else if (reset_all) {
+                        write = 1;
+                        set[0] = set[1] = set[2] = 0.0f;
+                    }
+                } else if (col->kind == 5) {
+                    if (act) {
+                        if (fabsf(o0) < wid && fabsf(o1) < wid && fabsf(o2) < wid) {
+                            write = 1;
+                            for (int c = 0; c < 3; ++c) set[c] = vel[c];
+                        }
+                    } else if (reset_all) {
+                        write = 1;
+                        set[0] = set[1] = set[2] = 0.0f;
+                    }
+                } else if (col->kind == 6) {
+                    if (act && sqrtf(o0 * o0 + o1 * o1 + o2 * o2) < rad) {
+                        write = 1;
+                        for (int c = 0; c < 3; ++c) set[c] = vel[c];
+                    }
+                }
+                if (write)
+                    for (int c = 0; c < 3; ++c) vv[c] = (real)set[c];
+            }
+}
+
 /* mpm_utils.py:241-306 */
 void PFX(g2p_apic_and_stress)(const OrcModel *m, int64_t np, real dt, const real *gvout,
                               real *x, real *v, real *C, real *F_trial, real *F, real *stress,
@@ -676,7 +783,8 @@ void PFX(p2g2p)(const OrcModel *m, PFX(State) * s, int64_t np, const OrcCollider
     PFX(grid_normalization_and_gravity)(m, dt, s->grid_m, s->grid_v_in, s->grid_v_out);
     for (int k = 0; k < ncol; ++k) {
         if (cols[k].kind == 0) PFX(collide_surface)(m, &cols[k], time, s->grid_v_out);
-        else PFX(collide_bounding_box)(m, &cols[k], time, s->grid_v_out);
+        else if (cols[k].kind == 1) PFX(collide_bounding_box)(m, &cols[k], time, s->grid_v_out);
+        else PFX(collide_extended)(m, &cols[k], time, dt, s->grid_v_out);
     }
     PFX(g2p_apic_and_stress)(m, np, dt, s->grid_v_out, s->x, s->v, s->C, s->F_trial, s->F,
                              s->stress, s->yield, status);

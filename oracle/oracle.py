@@ -49,6 +49,17 @@ class OrcCollider(C.Structure):
         ("friction", C.c_double),
         ("start_time", C.c_double),
         ("end_time", C.c_double),
+        ("reset", C.c_int32),
+        ("pad", C.c_int32),
+        ("velocity", C.c_double * 3),
+        ("threshold", C.c_double),
+        ("radius", C.c_double),
+        ("width", C.c_double),
+        ("height", C.c_double),
+        ("v_scale", C.c_double),
+        ("x_unit", C.c_double * 3),
+        ("y_unit", C.c_double * 3),
+        ("R", C.c_double),
     ]
 
 
@@ -138,6 +149,87 @@ def bounding_box(start_time=0.0, end_time=999.0) -> OrcCollider:
     return col
 
 
+def _f32(x) -> float:
+    """the value a wp.vec3 / float field of Dirichlet_collider holds"""
+    return float(np.float32(x))
+
+
+def _moving(kind, point, start_time, end_time, **kw) -> OrcCollider:
+    col = OrcCollider()
+    col.kind = kind
+    for c in range(3):
+        col.point[c] = _f32(point[c])
+    col.start_time = _f32(start_time)
+    col.end_time = _f32(end_time)
+    for k, v in kw.items():
+        if isinstance(v, (tuple, list)):
+            for c in range(3):
+                getattr(col, k)[c] = _f32(v[c])
+        else:
+            setattr(col, k, v if k == "reset" else _f32(v))
+    return col
+
+
+def _unit(v):
+    scale = 1.0 / math.sqrt(sum(x * x for x in v))
+    return [scale * x for x in v]
+
+
+def velocity_plane(point, normal, velocity, threshold, start_time=0.0, end_time=999.0, reset=0):
+    """engine_stress/mpm_solver_warp.py:527-543"""
+    return _moving(2, point, start_time, end_time, normal=_unit(normal), velocity=velocity,
+                   threshold=threshold, reset=int(reset))
+
+
+def circle_column(R, radius, height, v_scale, start_time=0.0, end_time=999.0):
+    """engine_stress/mpm_solver_warp.py:570-579"""
+    return _moving(3, (0.5, 0.069, 0.5 + R), start_time, end_time, radius=radius, height=height,
+                   v_scale=v_scale, R=R)
+
+
+def rotating_disk(point, normal, radius, width, v_scale, start_time=0.0, end_time=999.0, reset=0):
+    """engine_stress/mpm_solver_warp.py:609-633 (the axis search of :615-618
+    only ever tests normal[0]; other normals do not terminate there)"""
+    n = _unit(normal)
+    if not abs(n[0]) > 1e-1:
+        raise ValueError("normal[0] must exceed 0.1 in magnitude")
+    x = [1.0, 1.0, 1.0]
+    x[0] = -(n[0] + n[1] + n[2] - n[0]) / n[0]
+    y = list(np.cross(np.array(n), np.array(x)))
+    return _moving(4, point, start_time, end_time, normal=n, x_unit=_unit(x), y_unit=_unit(y),
+                   radius=radius, width=width, v_scale=v_scale, reset=int(reset))
+
+
+def velocity_cube(point, width, velocity, start_time=0.0, end_time=999.0, reset=0):
+    """engine_stress/mpm_solver_warp.py:667-679"""
+    return _moving(5, point, start_time, end_time, width=width, velocity=velocity, reset=int(reset))
+
+
+def sphere_leader(center, radius, velocity, start_time=0.0, end_time=999.0):
+    """engine_stress/mpm_solver_warp.py:697-707"""
+    return _moving(6, center, start_time, end_time, radius=radius, velocity=velocity)
+
+
+def advance_collider(col: OrcCollider, time: float, dt: float) -> None:
+    """The reference's modify_bc callbacks (mpm_solver_warp.py:561-565,
+    :594-603, :690-693, :716-718), run on the host after each substep's
+    collider kernels: time and dt in double, the point stored back in float."""
+    if col.kind not in (2, 3, 5, 6) or not (time >= col.start_time and time < col.end_time):
+        return
+    if col.kind == 3:
+        f = np.float32
+        z0, z1, z2 = f(col.point[0]) - f(0.5), f(col.point[1]), f(col.point[2]) - f(0.5)
+        c = z0 / np.sqrt(z0 * z0 + z1 * z1 + z2 * z2)
+        th = np.arccos(np.clip(c, f(-1), f(1)))
+        if z2 < 0:
+            th = -th
+        vel = (f(-col.v_scale) * np.sin(th), f(0.0), f(col.v_scale) * np.cos(th))
+    else:
+        vel = tuple(col.velocity)
+    for c in range(3):
+        col.point[c] = _f32(col.point[c] + dt * float(vel[c]))
+
+
 class OracleSim:
     """Reference-layout simulator state advanced by the C oracle."""
 
@@ -195,6 +287,8 @@ class OracleSim:
         self._fn("p2g2p")(C.byref(self.model), C.byref(s), C.c_int64(self.n), arr, C.c_int(ncol),
                           C.c_double(self.time), self._real(dt), C.c_int(nthreads_p2g),
                           C.byref(self.status))
+        for col in self.colliders:
+            advance_collider(col, self.time, dt)
         self.time = self.time + dt
 
     # ---- individual kernels (same order as p2g2p) for per-stage checks ----
@@ -214,9 +308,15 @@ class OracleSim:
                                                    _ptr(self.grid_m), _ptr(self.grid_v_in),
                                                    _ptr(self.grid_v_out))
         for col in self.colliders:
+            if col.kind >= 2:
+                self._fn("collide_extended")(C.byref(self.model), C.byref(col), C.c_double(self.time),
+                                             self._real(dt), _ptr(self.grid_v_out))
+                continue
             name = "collide_surface" if col.kind == 0 else "collide_bounding_box"
             self._fn(name)(C.byref(self.model), C.byref(col), C.c_double(self.time),
                            _ptr(self.grid_v_out))
+        for col in self.colliders:
+            advance_collider(col, self.time, dt)
 
     def stage_g2p(self, dt: float) -> None:
         self._fn("g2p_apic_and_stress")(C.byref(self.model), C.c_int64(self.n), self._real(dt),

@@ -15,7 +15,10 @@ MPM_MAX_COLLIDERS = 8
 MPM_OK, MPM_ERR_ARG, MPM_ERR_CUDA, MPM_ERR_SIZE = 0, -1, -2, -3
 ST_OUT_OF_DOMAIN, ST_CFL, ST_NONFINITE, ST_INTERNAL = 1, 2, 4, 8
 JELLY, METAL, SAND = 0, 1, 2
-COLLIDER_SURFACE, COLLIDER_BOX = 0, 1
+(COLLIDER_SURFACE, COLLIDER_BOX, COLLIDER_VPLANE, COLLIDER_CIRCLE, COLLIDER_DISK, COLLIDER_CUBE,
+ COLLIDER_SPHERE) = range(7)
+MOVING_COLLIDERS = (COLLIDER_VPLANE, COLLIDER_CIRCLE, COLLIDER_CUBE, COLLIDER_SPHERE)
+CF_EXTENDED, CF_MOVING = 1, 2
 MLP_IN, MLP_OUT, MLP_HIDDEN, MLP_PARAMS = 12, 6, 128, 37264
 
 (FIELD_X_INITIAL, FIELD_U, FIELD_V, FIELD_C, FIELD_F, FIELD_STRESS, FIELD_MASS, FIELD_VOL,
@@ -33,7 +36,10 @@ STATUS_NAMES = {ST_OUT_OF_DOMAIN: "particle stencil outside the grid (particle f
 class MpmCollider(C.Structure):
     _fields_ = [("kind", C.c_int32), ("surface_type", C.c_int32), ("point", C.c_float * 3),
                 ("normal", C.c_float * 3), ("friction", C.c_float), ("start_time", C.c_float),
-                ("end_time", C.c_float), ("pad0", C.c_float)]
+                ("end_time", C.c_float), ("reset", C.c_int32), ("velocity", C.c_float * 3),
+                ("threshold", C.c_float), ("radius", C.c_float), ("width", C.c_float),
+                ("height", C.c_float), ("v_scale", C.c_float), ("x_unit", C.c_float * 3),
+                ("y_unit", C.c_float * 3), ("R", C.c_float), ("pad0", C.c_float)]
 
 
 class MpmScene(C.Structure):
@@ -55,7 +61,7 @@ class MpmPlan(C.Structure):
 class MpmBuffers(C.Structure):
     _fields_ = [("state", C.c_void_p * 2), ("workspace", C.c_void_p), ("scenes", C.c_void_p),
                 ("status", C.c_void_p), ("plan", MpmPlan), ("cur", C.c_int32),
-                ("keys_valid", C.c_int32), ("reserved0", C.c_int32), ("pad0", C.c_int32),
+                ("keys_valid", C.c_int32), ("collider_flags", C.c_int32), ("pad0", C.c_int32),
                 ("substep", C.c_int64)]
 
 

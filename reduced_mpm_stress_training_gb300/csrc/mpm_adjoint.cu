@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(256) grid_adjoint_kernel(const MpmScene *__res
                     v[0] = v[1] = v[2] = 0.0f;
                     keep[0] = keep[1] = keep[2] = 0.0f;
                 }
-            } else {
+            } else if (cl.kind == MPM_COLLIDER_BOX) {  // (other kinds are refused by mpm_adjoint_substep)
                 const int id[3] = {ix, iy, iz};
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {

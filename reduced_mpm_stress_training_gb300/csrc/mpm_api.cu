@@ -223,6 +223,19 @@ int mpm_init(MpmBuffers *b, void *stream) {
 
 int mpm_upload_scenes(MpmBuffers *b, const MpmScene *scenes, int32_t n_scenes, void *stream) {
     if (!b || !b->scenes || !scenes || n_scenes != b->plan.n_scenes) return MPM_ERR_ARG;
+    int flags = 0;
+    for (int s = 0; s < n_scenes; ++s) {
+        if (scenes[s].n_colliders < 0 || scenes[s].n_colliders > MPM_MAX_COLLIDERS) return MPM_ERR_ARG;
+        for (int k = 0; k < scenes[s].n_colliders; ++k) {
+            const int kind = scenes[s].colliders[k].kind;
+            if (kind < MPM_COLLIDER_SURFACE || kind > MPM_COLLIDER_SPHERE) return MPM_ERR_ARG;
+            if (kind >= MPM_COLLIDER_VPLANE) flags |= MPM_CF_EXTENDED;
+            if (kind == MPM_COLLIDER_VPLANE || kind == MPM_COLLIDER_CIRCLE || kind == MPM_COLLIDER_CUBE ||
+                kind == MPM_COLLIDER_SPHERE)
+                flags |= MPM_CF_MOVING;
+        }
+    }
+    b->collider_flags = flags;
     MPM_CHECK(cudaMemcpyAsync(b->scenes, scenes, sizeof(MpmScene) * (size_t)n_scenes,
                               cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream)));
     return MPM_OK;
@@ -377,6 +390,9 @@ int mpm_p2g(MpmBuffers *b, float dt, void *stream) {
 int mpm_grid_update(MpmBuffers *b, float time, float dt, void *stream) {
     if (!buffers_ok(b)) return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_grid(make_ctx(b, stream, b->cur), time, dt));
+    if (b->collider_flags & MPM_CF_MOVING)  // after every node used the old points
+        MPM_CHECK(mpm::launch_advance_colliders(static_cast<MpmScene *>(b->scenes), b->plan.n_scenes, time, dt,
+                                                static_cast<cudaStream_t>(stream)));
     return MPM_OK;
 }
 
@@ -462,6 +478,7 @@ int mpm_adjoint_substep(MpmBuffers *b, const float *adj_out, float *adj_in, void
     if (!buffers_ok(b) || !theta_bar || !grid_adj) return MPM_ERR_ARG;
     if (b->plan.n_particles > 0 && (!adj_out || !adj_in || adj_out == adj_in)) return MPM_ERR_ARG;
     if (reinterpret_cast<uintptr_t>(grid_adj) & 15) return MPM_ERR_ARG;
+    if (b->collider_flags & MPM_CF_EXTENDED) return MPM_ERR_ARG;  // surface and box colliders only
     MPM_CHECK(mpm::launch_adjoint(make_ctx(b, stream, b->cur), adj_out, adj_in, static_cast<float4 *>(grid_adj),
                                   theta_bar, time, dt));
     return MPM_OK;

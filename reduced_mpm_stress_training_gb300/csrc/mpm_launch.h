@@ -62,6 +62,7 @@ cudaError_t launch_features(const MpmScene &scene, const float *F, const float *
 cudaError_t launch_init_state(const Ctx &cx, const PState &other);
 cudaError_t launch_load(const Ctx &cx, int field, const float *src);
 cudaError_t launch_export(const Ctx &cx, int field, float *dst);
+cudaError_t launch_advance_colliders(MpmScene *scenes, int n_scenes, float time, float dt, cudaStream_t stream);
 cudaError_t launch_load_uvstress(const Ctx &cx, const float *u, const float *v, const float *tau);
 cudaError_t launch_export_uvFstress(const Ctx &cx, float *u, float *v, float *fd, float *tau);
 cudaError_t launch_export_grid(const Ctx &cx, const MpmScene &host_scene, int scene_index,

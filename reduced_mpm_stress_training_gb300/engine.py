@@ -54,7 +54,8 @@ def dp_alpha(friction_angle: float) -> float:
 
 @dataclasses.dataclass
 class Collider:
-    """Dirichlet_collider subset (engine_stress/warp_utils.py:126-151)."""
+    """Dirichlet_collider (engine_stress/warp_utils.py:126-151) of one of the
+    reference's grid boundary conditions (engine_stress/mpm_solver_warp.py:407-720)."""
     kind: int
     point: tuple = (0.0, 0.0, 0.0)
     normal: tuple = (0.0, 0.0, 1.0)
@@ -62,23 +63,81 @@ class Collider:
     friction: float = 0.0
     start_time: float = 0.0
     end_time: float = 999.0
+    reset: int = 0
+    velocity: tuple = (0.0, 0.0, 0.0)
+    threshold: float = 0.0
+    radius: float = 0.0
+    width: float = 0.0
+    height: float = 0.0
+    v_scale: float = 0.0
+    x_unit: tuple = (1.0, 0.0, 0.0)
+    y_unit: tuple = (0.0, 1.0, 0.0)
+    R: float = 0.0
+
+    @staticmethod
+    def _unit(v):
+        scale = 1.0 / math.sqrt(sum(x ** 2 for x in v))
+        return tuple(scale * x for x in v)
 
     @staticmethod
     def surface(point, normal, surface="sticky", friction=0.0, start_time=0.0, end_time=999.0):
         """engine_stress/mpm_solver_warp.py:407-428 (normal normalised, sticky needs friction 0)."""
-        point = list(point)
-        scale = 1.0 / math.sqrt(sum(x ** 2 for x in normal))
-        normal = [scale * x for x in normal]
         if surface == "sticky" and friction != 0:
             raise ValueError("friction must be 0 on sticky surfaces.")
         st = 0 if surface == "sticky" else (1 if surface == "slip" else 2)
-        return Collider(A.COLLIDER_SURFACE, tuple(point), tuple(normal), st, friction,
+        return Collider(A.COLLIDER_SURFACE, tuple(point), Collider._unit(normal), st, friction,
                         start_time, end_time)
 
     @staticmethod
     def bounding_box(start_time=0.0, end_time=999.0):
         """engine_stress/mpm_solver_warp.py:499-503"""
         return Collider(A.COLLIDER_BOX, start_time=start_time, end_time=end_time)
+
+    @staticmethod
+    def velocity_plane(point, normal, velocity, threshold, start_time=0.0, end_time=999.0, reset=0):
+        """engine_stress/mpm_solver_warp.py:527-543: the slab |(x - point).normal| <=
+        threshold takes `velocity` and moves with it."""
+        return Collider(A.COLLIDER_VPLANE, tuple(point), Collider._unit(normal), start_time=start_time,
+                        end_time=end_time, reset=int(reset), velocity=tuple(velocity),
+                        threshold=float(threshold))
+
+    @staticmethod
+    def circle_column(R, radius, height, v_scale, start_time=0.0, end_time=999.0):
+        """engine_stress/mpm_solver_warp.py:570-579: a vertical column (radius,
+        half-height) whose bottom point starts at (0.5, 0.069, 0.5 + R) and
+        circles about (0.5, *, 0.5) at speed v_scale."""
+        return Collider(A.COLLIDER_CIRCLE, (0.5, 0.069, 0.5 + R), start_time=start_time, end_time=end_time,
+                        radius=float(radius), height=float(height), v_scale=float(v_scale), R=float(R))
+
+    @staticmethod
+    def rotating_disk(point, normal, radius, width, v_scale, start_time=0.0, end_time=999.0, reset=0):
+        """engine_stress/mpm_solver_warp.py:609-633: in-plane axes from the
+        normalised normal as the reference builds them.  The reference's axis
+        search never advances past normal[0] (it loops forever when
+        |normal[0]| <= 0.1); that case raises here instead."""
+        n = Collider._unit(normal)
+        if not abs(n[0]) > 1e-1:
+            raise ValueError("set_rotation_on_disk needs |normal[0]| > 0.1 after normalisation "
+                             "(the reference's local-axis search does not terminate otherwise)")
+        x = [1.0, 1.0, 1.0]
+        x[0] = -(n[0] + n[1] + n[2] - n[0]) / n[0]
+        y = [n[1] * x[2] - n[2] * x[1], n[2] * x[0] - n[0] * x[2], n[0] * x[1] - n[1] * x[0]]
+        return Collider(A.COLLIDER_DISK, tuple(point), n, start_time=start_time, end_time=end_time,
+                        reset=int(reset), radius=float(radius), width=float(width), v_scale=float(v_scale),
+                        x_unit=Collider._unit(x), y_unit=Collider._unit(y))
+
+    @staticmethod
+    def velocity_cube(point, width, velocity, start_time=0.0, end_time=999.0, reset=0):
+        """engine_stress/mpm_solver_warp.py:667-679: nodes within `width` of
+        the point (each axis) take `velocity`; the cube moves with it."""
+        return Collider(A.COLLIDER_CUBE, tuple(point), start_time=start_time, end_time=end_time,
+                        reset=int(reset), velocity=tuple(velocity), width=float(width))
+
+    @staticmethod
+    def sphere(center, radius, velocity, start_time=0.0, end_time=999.0):
+        """engine_stress/mpm_solver_warp.py:697-707 (add_sphere_leader)."""
+        return Collider(A.COLLIDER_SPHERE, tuple(center), start_time=start_time, end_time=end_time,
+                        velocity=tuple(velocity), radius=float(radius))
 
     def to_struct(self) -> A.MpmCollider:
         c = A.MpmCollider()
@@ -87,9 +146,19 @@ class Collider:
         for i in range(3):
             c.point[i] = self.point[i]
             c.normal[i] = self.normal[i]
+            c.velocity[i] = self.velocity[i]
+            c.x_unit[i] = self.x_unit[i]
+            c.y_unit[i] = self.y_unit[i]
         c.friction = self.friction
         c.start_time = self.start_time
         c.end_time = self.end_time
+        c.reset = self.reset
+        c.threshold = self.threshold
+        c.radius = self.radius
+        c.width = self.width
+        c.height = self.height
+        c.v_scale = self.v_scale
+        c.R = self.R
         return c
 
 
@@ -173,6 +242,8 @@ class MPMEngine:
 
     def _allocate(self, fresh: bool) -> None:
         """Plan and allocate; fresh=False keeps the particle state (grid change)."""
+        if not fresh:
+            self._sync_moving_colliders()
         table = self._scene_table()
         plan = A.MpmPlan()
         A.check(self.lib.mpm_plan(table, len(self.scenes), self.n_particles, self.chunk_size,
@@ -198,13 +269,26 @@ class MPMEngine:
         b.status = self._status.data_ptr()
         b.plan = plan
         self.buf = b
-        self._upload()
+        self._upload(sync=False)  # moving points were read back above (the device table is new)
         if fresh:
             A.check(self.lib.mpm_init(C.byref(b), self.stream), "mpm_init")
         else:
             b.keys_valid = 0  # block keys depend on the grid
 
-    def _upload(self) -> None:
+    def _sync_moving_colliders(self) -> None:
+        """Moving colliders advance on the device (mpm_grid_update); copy their
+        current points back into the scene parameters before a re-upload."""
+        if getattr(self, "table", None) is None or not (self.buf.collider_flags & A.CF_MOVING):
+            return
+        dev = (A.MpmScene * len(self.scenes)).from_buffer_copy(self._scenes_dev.cpu().numpy().tobytes())
+        for i, sp in enumerate(self.scenes):
+            for k, c in enumerate(sp.colliders[:dev[i].n_colliders]):
+                if c.kind in A.MOVING_COLLIDERS and dev[i].colliders[k].kind == c.kind:
+                    c.point = tuple(float(x) for x in dev[i].colliders[k].point)
+
+    def _upload(self, sync: bool = True) -> None:
+        if sync:
+            self._sync_moving_colliders()
         table = self._scene_table()
         A.check(self.lib.mpm_plan(table, len(self.scenes), self.n_particles, self.chunk_size,
                                   C.byref(A.MpmPlan())), "mpm_plan")

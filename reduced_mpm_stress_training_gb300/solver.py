@@ -18,8 +18,13 @@ the current PyTorch CUDA stream.  Differences a caller can see:
   ``load_from_sampling`` sets it to I, :149).
 * Extensions: ``set_parameters(E=, nu=, gravity=(gx,gy,gz), particle_vol=)``,
   ``load_vol_from_tensor``, ``load_F_from_tensor``, ``load_yield_from_tensor``.
-* Colliders other than the surface collider and the bounding box raise
-  NotImplementedError.
+* All the reference's colliders are built.  Moving ones advance on the
+  device after each active substep's grid update; their host-side
+  parameters are refreshed from the device when the scene is re-uploaded.
+  ``set_rotation_on_disk`` raises ValueError for |normal[0]| <= 0.1 (the
+  reference's axis search loops forever there) and gives v = 0 to nodes on
+  the disk axis (the reference divides 0 by 0).  The reduced
+  sampled-quadrature substep ``p2g2p_reduced`` raises NotImplementedError.
 """
 from __future__ import annotations
 
@@ -264,17 +269,39 @@ class MPMSimulator:
         self._params.colliders.append(Collider.bounding_box(start_time, end_time))
         self._engine.update_scenes()
 
-    def _not_built(self, *a, **k):
-        raise NotImplementedError("this collider is outside the GB300 substep's scope "
-                                  "(only add_surface_collider and add_bounding_box are built)")
+    def _add_collider(self, c: Collider) -> None:
+        self._params.colliders.append(c)
+        self._engine.update_scenes()
 
-    add_surface_collider2 = _not_built
-    set_velocity_on_infinite_plane = _not_built
-    set_column_moving_as_circle = _not_built
-    set_rotation_on_disk = _not_built
-    set_velocity_on_cube = _not_built
-    add_sphere_leader = _not_built
-    p2g2p_reduced = _not_built
+    # add_surface_collider2 (mpm_solver_warp.py:453-497) writes zero for every
+    # surface type too (:495): the same collider
+    add_surface_collider2 = add_surface_collider
+
+    def set_velocity_on_infinite_plane(self, point, normal, velocity, threshold, start_time=0.0, end_time=999.0,
+                                       reset=0):
+        """engine_stress/mpm_solver_warp.py:527-568"""
+        self._add_collider(Collider.velocity_plane(point, normal, velocity, threshold, start_time, end_time, reset))
+
+    def set_column_moving_as_circle(self, R, radius, height, v_scale, start_time=0.0, end_time=999.0):
+        """engine_stress/mpm_solver_warp.py:570-607"""
+        self._add_collider(Collider.circle_column(R, radius, height, v_scale, start_time, end_time))
+
+    def set_rotation_on_disk(self, point, normal, radius, width, v_scale, start_time=0.0, end_time=999.0, reset=0):
+        """engine_stress/mpm_solver_warp.py:609-665"""
+        self._add_collider(Collider.rotating_disk(point, normal, radius, width, v_scale, start_time, end_time,
+                                                  reset))
+
+    def set_velocity_on_cube(self, point, width, velocity, start_time=0.0, end_time=999.0, reset=0):
+        """engine_stress/mpm_solver_warp.py:667-695"""
+        self._add_collider(Collider.velocity_cube(point, width, velocity, start_time, end_time, reset))
+
+    def add_sphere_leader(self, center, radius, velocity, start_time=0, end_time=999):
+        """engine_stress/mpm_solver_warp.py:697-720"""
+        self._add_collider(Collider.sphere(center, radius, velocity, start_time, end_time))
+
+    def p2g2p_reduced(self, *a, **k):
+        raise NotImplementedError("the reduced sampled-quadrature substep is outside the GB300 "
+                                  "substep's scope")
 
 
 MPM_Simulator_WARP = MPMSimulator

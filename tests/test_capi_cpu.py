@@ -42,7 +42,7 @@ def test_struct_sizes_match_binding(built):
     lib.mpm_struct_sizes(out)
     assert list(out) == [C.sizeof(A.MpmCollider), C.sizeof(A.MpmScene), C.sizeof(A.MpmPlan),
                          C.sizeof(A.MpmBuffers)]
-    assert lib.mpm_abi_version() == 1
+    assert lib.mpm_abi_version() == 2
 
 
 def _plan(scenes, n, chunk=128):

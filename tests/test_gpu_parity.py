@@ -456,3 +456,64 @@ def test_tilted_timed_colliders_match_oracle(cuda):
         moved.append(float(np.abs(gpu_state(sim)["v"]).max()))
     assert sim.check_status() == 0
     assert max(moved) > 0.0
+
+
+# the reference's other grid boundary conditions (mpm_solver_warp.py:527-720):
+# (simulator method, oracle factory, keyword arguments); windows end between
+# substeps so the reset rules run too
+_EXTENDED_COLLIDERS = {
+    "velocity_plane": ("set_velocity_on_infinite_plane", "velocity_plane",
+                       dict(point=(0.5, 0.5, 0.3), normal=(0.2, 0.1, 1.0), velocity=(0.0, 0.1, 0.4),
+                            threshold=0.03, start_time=0.0, end_time=6.5e-4, reset=1)),
+    "circle_column": ("set_column_moving_as_circle", "circle_column",
+                      dict(R=0.1, radius=0.08, height=0.5, v_scale=0.5, start_time=0.0, end_time=999.0)),
+    "rotating_disk": ("set_rotation_on_disk", "rotating_disk",
+                      dict(point=(0.5, 0.5, 0.45), normal=(1.0, 0.15, 0.1), radius=0.12, width=0.05,
+                           v_scale=5.0, start_time=1.5e-4, end_time=6.5e-4, reset=1)),
+    "velocity_cube": ("set_velocity_on_cube", "velocity_cube",
+                      dict(point=(0.5, 0.5, 0.4), width=0.06, velocity=(0.3, 0.0, 0.2), start_time=0.0,
+                           end_time=6.5e-4, reset=1)),
+    "sphere_leader": ("add_sphere_leader", "sphere_leader",
+                      dict(center=(0.45, 0.5, 0.5), radius=0.07, velocity=(0.5, 0.0, -0.3), start_time=0.0,
+                           end_time=999.0)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(_EXTENDED_COLLIDERS))
+def test_extended_colliders_match_oracle(cuda, name):
+    """Each of the reference's other colliders, moving ones included, over 10
+    substeps against the oracle; halfway through a bounding box is added,
+    which re-uploads the scene table and must keep the moving collider where
+    the device advanced it."""
+    method, factory, kw = _EXTENDED_COLLIDERS[name]
+    sc = S.small_column(8192, 32)
+    dt = sc.dt
+    x0, v0, vol, mass = sc.particles()
+    sim = gpu_sim(sc, x0=x0, v0=v0, vol=vol, mass=mass, colliders=False)
+    getattr(sim, method)(**kw)
+    m = O.make_model(sc.n_grid, sc.grid_lim, material=sc.material, E=sc.E, nu=sc.nu,
+                     friction_angle=sc.friction_angle, gravity=sc.gravity)
+    refs = [O.OracleSim(m, x0, mass, vol, v0, bits=b, colliders=[getattr(O, factory)(**kw)]) for b in (32, 64)]
+    for k in range(10):
+        if k == 5:
+            sim.add_bounding_box()
+            for r in refs:
+                r.colliders.append(O.bounding_box())
+        sim.p2g2p(k, dt)
+        for r in refs:
+            r.p2g2p(dt)
+        errs = compare(sim, refs[0], fields=("x", "v", "F"))
+        tol = _step_tol(refs[0], refs[1], errs)
+        assert all(errs[f] < tol[f] for f in errs), (name, k, errs, tol)
+    assert sim.check_status() == 0
+    col = sim._params.colliders[0]
+    sim._engine.update_scenes()  # reads the device-side point back
+    ref_col = refs[0].colliders[0]
+    assert np.allclose(col.point, tuple(ref_col.point), rtol=0, atol=1e-6), (col.point, tuple(ref_col.point))
+
+
+def test_disk_with_small_normal_x_is_refused(cuda):
+    sc = S.small_column(64, 16)
+    sim = gpu_sim(sc)
+    with pytest.raises(ValueError):
+        sim.set_rotation_on_disk((0.5, 0.5, 0.5), (0.05, 1.0, 0.0), 0.1, 0.05, 1.0)

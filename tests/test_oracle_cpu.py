@@ -196,3 +196,52 @@ def test_out_of_domain_is_flagged_and_frozen():
     sim.p2g2p(sc.dt)
     assert sim.status.value & O.ST_OUT_OF_DOMAIN
     assert np.all(sim.u[3] == 0) and np.all(sim.F[3] == np.eye(3, dtype=np.float32).ravel())
+
+
+def _collide(col, n=16, time=1e-4, dt=1e-4):
+    """The oracle's collider kernel on a zero velocity grid (float32 build)."""
+    import ctypes as C
+    m = O.make_model(n, 1.0, material="sand", E=2e5, nu=0.3)
+    gv = np.zeros(n ** 3 * 3, dtype=np.float32)
+    O.lib(32).orc32_collide_extended(C.byref(m), C.byref(col), C.c_double(time), C.c_float(dt),
+                                     gv.ctypes.data_as(C.c_void_p))
+    idx = np.stack(np.meshgrid(*[np.arange(n)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    return gv.reshape(-1, 3), idx.astype(np.float32) * np.float32(1.0 / n)
+
+
+def test_oracle_extended_colliders_known_answers():
+    """Region and velocity of each extended collider kernel on a 16^3 grid
+    (engine_stress/mpm_solver_warp.py:527-720), and the host-side motion."""
+    f = np.float32
+    # sphere: |x - c| < r takes the velocity
+    col = O.sphere_leader((0.5, 0.5, 0.5), 0.2, (1.0, -2.0, 0.5))
+    v, x = _collide(col)
+    inside = np.sqrt(((x - f(0.5)) ** 2).sum(1)) < f(0.2)
+    assert inside.sum() > 0 and np.all(v[inside] == np.float32([1.0, -2.0, 0.5])) and np.all(v[~inside] == 0)
+    # cube: every axis within the half-width
+    col = O.velocity_cube((0.4, 0.5, 0.6), 0.13, (0.0, 0.0, 3.0))
+    v, x = _collide(col)
+    inside = np.all(np.abs(x - f([0.4, 0.5, 0.6])) < f(0.13), axis=1)
+    assert inside.sum() == 4 * 5 * 4 and np.all(v[inside, 2] == 3.0) and np.all(v[~inside] == 0)
+    # plane: the slab |(x - p).n| <= threshold
+    col = O.velocity_plane((0.5, 0.5, 0.5), (0.0, 0.0, 1.0), (0.0, 1.0, 0.0), 0.07)
+    v, x = _collide(col)
+    inside = np.abs(x[:, 2] - f(0.5)) <= f(0.07)
+    assert inside.sum() == 3 * 256 and np.all(v[inside, 1] == 1.0) and np.all(v[~inside] == 0)
+    # disk about x: rigid rotation v = v_scale n x r with r = (0, y, z) - p
+    col = O.rotating_disk((0.5, 0.5, 0.5), (1.0, 0.0, 0.0), 0.3, 0.07, 4.0)
+    v, x = _collide(col)
+    r = x - f(0.5)
+    inside = (np.abs(r[:, 0]) < f(0.07)) & (np.sqrt(r[:, 1] ** 2 + r[:, 2] ** 2) < f(0.3))
+    r[:, 0] = 0
+    expect = 4.0 * np.cross(np.array([1.0, 0.0, 0.0]), r)
+    assert inside.sum() > 0 and np.allclose(v[inside], expect[inside], atol=1e-5)
+    assert np.all(v[~inside] == 0)
+    # the moving kinds advance by dt v while active, in float
+    col = O.sphere_leader((0.5, 0.5, 0.5), 0.2, (1.0, -2.0, 0.5), start_time=0.0, end_time=1e-3)
+    O.advance_collider(col, 0.0, 1e-4)
+    assert tuple(col.point) == tuple(float(f(a + 1e-4 * b)) for a, b in zip((0.5, 0.5, 0.5), (1.0, -2.0, 0.5)))
+    O.advance_collider(col, 2e-3, 1e-4)  # outside its window: stays
+    assert tuple(col.point) == tuple(float(f(a + 1e-4 * b)) for a, b in zip((0.5, 0.5, 0.5), (1.0, -2.0, 0.5)))
+    with pytest.raises(ValueError):
+        O.rotating_disk((0.5, 0.5, 0.5), (0.05, 1.0, 0.0), 0.3, 0.07, 4.0)
