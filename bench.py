@@ -15,6 +15,8 @@ One JSON line on rank 0.  A "step" is one substep of every particle.
             loads u, v, stress from pinned host memory (load_uvstress_from_tensor),
             runs the substep and reads u, v, F_disp, stress back to pinned host
             memory (export_uvFstress_from_warp)
+  --workload reduced_1m -- the reduced sampled-quadrature substep
+            (p2g2p_reduced) on the same column with 4,096 sample points
   --impl reference -- the CPU restatement of the reference's algorithm (the
             reference is Python + Warp and cannot be installed here) on all
             host cores, on a bounded particle sample per step.
@@ -542,6 +544,108 @@ def batched_arm(args):
                       "speedup_vs_one_by_one": seq / t, "status": b.engine.status()}), flush=True)
 
 
+def reduced_arm(args):
+    """The reduced sampled-quadrature substep (MPM_Simulator_WARP.p2g2p_reduced) on the
+    large sand column after two plain substeps, with 4,096 seeded sample points:
+    every particle is scanned, the marked ones scatter, and the dense 128^3 grid is
+    written.  Substeps are replayed from a CUDA graph and timed with CUDA events."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as g
+    from reduced_mpm_stress_training_gb300 import MPM_Simulator_WARP
+    from reduced_mpm_stress_training_gb300 import _capi as A
+    from reduced_mpm_stress_training_gb300 import scenarios as S
+
+    g.build()
+    sc = S.sand_column_1m()
+    n, ng, dt = sc.n_particles, sc.n_grid, sc.dt
+    device = torch.device("cuda:0")
+    x0, v0, vol, mass = sc.particles()
+    sim = MPM_Simulator_WARP(n, n_grid=ng, grid_lim=sc.grid_lim, device=device)
+    sim.set_parameters(material=sc.material, E=sc.E, nu=sc.nu, friction_angle=sc.friction_angle,
+                       gravity=sc.gravity)
+    sim.load_x_initial_from_tensor(torch.from_numpy(x0))
+    sim.load_vol_from_tensor(torch.from_numpy(vol))
+    sim.set_parameters(density=sc.density)
+    sim.load_v_from_tensor(torch.from_numpy(v0))
+    for kind, kw in sc.colliders():
+        sim.add_surface_collider(**kw) if kind == "surface" else sim.add_bounding_box(**kw)
+    for k in range(2):
+        sim.p2g2p(k, dt)
+    n_samples = 4096
+    sample = np.random.default_rng(0).choice(n, n_samples, replace=False).astype(np.int32)
+    sim.load_sample_particle_index_from_tensor(torch.from_numpy(sample))
+    for k in range(max(3, args.warmup)):
+        sim.p2g2p_reduced(k, dt)
+    sim.check_status()
+    rg = sim._reduced_grid()
+    rg.f_disp = sim._f_disp_state()
+    gs = rg.struct(sim.engine)
+    lib, buf = A.load(), sim.engine.buf
+    gsize = 16
+    graph, side = torch.cuda.CUDAGraph(), torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=side):
+        hs = torch.cuda.current_stream().cuda_stream
+        for _ in range(gsize):  # time and moving colliders are fixed: the scene has none that move
+            A.check(lib.mpm_p2g2p_reduced(C.byref(buf), C.byref(gs), float(sim.time), dt, hs),
+                    "mpm_p2g2p_reduced")
+    graph.replay()
+    torch.cuda.synchronize()
+    K = max(gsize, min(args.steps, 2000) // gsize * gsize)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(K // gsize):
+        graph.replay()
+    e1.record(st)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / K
+    # algorithmic bytes of one reduced substep: every particle's x_initial, u and the mark
+    # of its base cell (28 B); a marked particle's F_disp, density, v, mass read and F
+    # written (92 B); every node's scratch cleared and read, both marks cleared, the mark
+    # read, grid_m, grid_v_in, grid_v_out written (76 B)
+    x = sim.engine.export(A.FIELD_X).reshape(n, 3)
+    base = torch.trunc(x * np.float32(ng) - 0.5).long()
+    marked = int((rg.neighboring_cells[base[:, 0], base[:, 1], base[:, 2]] > 0).sum())
+    alg = 28 * n + 92 * marked + 76 * ng ** 3
+    peak, peak_src = measured_peak_hbm()
+    achieved = alg / t / 1e9
+    # CPU restatement of the same step (single-threaded), one substep on the same state
+    from oracle import oracle as O
+
+    m = O.make_model(ng, sc.grid_lim, material=sc.material, E=sc.E, nu=sc.nu,
+                     friction_angle=sc.friction_angle, gravity=sc.gravity)
+    cols = [O.surface_collider(**kw) if k == "surface" else O.bounding_box(**kw) for k, kw in sc.colliders()]
+    ref = O.OracleSim(m, x0, mass, vol, v0, bits=32, colliders=cols)
+    ref.u[:] = sim.engine.export(A.FIELD_U).reshape(n, 3).cpu().numpy()
+    ref.v[:] = sim.engine.export(A.FIELD_V).reshape(n, 3).cpu().numpy()
+    ref.F_disp[:] = rg.f_disp.reshape(n, 9).cpu().numpy()
+    ref.density[:] = sc.density
+    ref.sample_particle_index_short = sample
+    t0 = time.perf_counter()
+    ref.p2g2p_reduced(dt)
+    cpu_t = time.perf_counter() - t0
+    print(json.dumps({
+        "metric": "particle-substeps/s (reduced sampled-quadrature substep, 1M sand, 4096 samples, fp32)",
+        "value": n / t, "unit": "particle-substeps/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"sand_column_1m after 2 substeps: {n} particles, {ng}^3 grid, "
+                               f"{n_samples} sample points, p2g2p_reduced",
+                   "marked_particles": marked, "marked_cells": int(rg.neighboring_cells.sum()),
+                   "l2": "inputs and dense grids larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src, "scope": "whole substep",
+                     "alg_bytes_per_step": alg},
+        "cpu_baseline": {"value": n / cpu_t, "unit": "particle-substeps/s", "cores": 1, "kind": "port",
+                         "sample": "one reduced substep of the same state (oracle, float32)"},
+        "status": sim.engine.status()}), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
@@ -550,6 +654,10 @@ def main():
     if args.workload == "batch_64":
         if rank == 0 and args.impl == "gb300":
             batched_arm(args)
+        return
+    if args.workload == "reduced_1m":
+        if rank == 0 and args.impl == "gb300":
+            reduced_arm(args)
         return
     sc = S.SCENES[args.workload]()
     if world > 1:

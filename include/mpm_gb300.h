@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 2
+#define MPM_ABI_VERSION 3
 #define MPM_MAX_COLLIDERS 8
 
 /* return codes */
@@ -41,6 +41,8 @@ extern "C" {
 #define MPM_ST_CFL 2           /* |v_i| > dx/dt (mpm_solver_warp.py:188-192)          */
 #define MPM_ST_NONFINITE 4     /* non-finite F or stress after the return map         */
 #define MPM_ST_INTERNAL 8      /* a particle was not inside its sorted block (bug)    */
+#define MPM_ST_BAD_INPUT 16    /* reduced substep: a sample index outside [0, n) or a
+                                  dense grid whose n_grid is not the scene's: skipped */
 
 /* material ids, engine_stress/mpm_solver_warp.py:90-94 */
 #define MPM_JELLY 0
@@ -250,6 +252,64 @@ int mpm_export_grid(MpmBuffers *b, int32_t scene, float *grid_m, float *grid_v_i
  * allocates. */
 int mpm_p2g2p_noalloc(MpmBuffers *b, float time, float dt, void *stream);
 
+/* ---- reduced sampled-quadrature substep ------------------------------
+ * MPM_Simulator_WARP.p2g2p_reduced (engine_stress/mpm_solver_warp.py:214-227)
+ * and its kernels (engine_stress/mpm_utils.py:318-471): only particles whose
+ * stencil base cell lies within two cells of a sample point's base cell
+ * scatter, with a stress recomputed from F_disp, into a dense grid that is
+ * the product of the call.  Single-scene plans only (MPM_ERR_ARG otherwise).
+ * Every array is the caller's device memory in the reference's own layout
+ * (warp_utils.py:84-124): particle arrays in the user's particle order,
+ * grids dense (n, n, n) C-order, flat index (ix * n + iy) * n + iz. */
+typedef struct MpmReducedGrid {
+    const int32_t *sample_index; /* n_samples user particle indices:
+                                    sample_particle_index_short             */
+    int64_t n_samples;
+    float *f_disp;               /* (n, 9) particle_F_disp: read by the P2G,
+                                    written for the samples by mpm_g2p_sample */
+    const float *density;        /* (n) particle_density                    */
+    void *grid_acc;              /* n^3 x 16 B scratch (momentum, mass)     */
+    float *grid_m;               /* n^3       written by mpm_p2g2p_reduced  */
+    float *grid_v_in;            /* n^3 x 3   momentum, same                */
+    float *grid_v_out;           /* n^3 x 3   velocity after the colliders  */
+    int32_t *neighboring_cells;        /* n^3 marks of the P2G (:318-335)    */
+    int32_t *neighboring_cells_grid_v; /* n^3 marks for the gather (:338-351) */
+    int32_t n_grid;              /* n: must equal the scene's n_grid        */
+    int32_t pad0;
+} MpmReducedGrid; /* 88 bytes */
+
+/* p2g2p_reduced (mpm_solver_warp.py:214-227): zero the grids and both mark
+ * arrays; mark the 5^3 cells around each sample point's base cell
+ * (update_neighboring_cells, mpm_utils.py:318-335); every particle whose
+ * base cell is marked sets F = F_disp + I (written to its state), takes the
+ * FCR (jelly, metal) or Drucker-Prager (sand) Kirchhoff stress of that F and
+ * scatters momentum w m v (no affine term), mass and the force
+ * -dt (m / density) stress grad w (p2g_sample_all, :353-402); marked nodes
+ * with m > 1e-10 get v_out = v_in / m + dt g, the others 0
+ * (grid_normalization_and_gravity_sample_all, :405-413); then the scene's
+ * colliders sweep every node and moving ones advance.  Particles are not
+ * moved; the caller advances time by dt, as for mpm_p2g2p.  A marked
+ * particle whose stencil would leave the grid, or any particle whose base
+ * cell is outside it (the reference indexes out of bounds there), is skipped
+ * and sets MPM_ST_OUT_OF_DOMAIN. */
+int mpm_p2g2p_reduced(MpmBuffers *b, const MpmReducedGrid *g, float time, float dt, void *stream);
+
+/* MPM_Simulator_WARP.experiment_for_C (mpm_solver_warp.py:207-209): mark
+ * neighboring_cells_grid_v over offsets -2..4 of each sample point's base
+ * cell (update_neighboring_cells_for_grid_v, mpm_utils.py:338-351).  Adds
+ * marks: the array is cleared only by mpm_p2g2p_reduced, as zero_grid does. */
+int mpm_mark_neighboring_cells_grid_v(MpmBuffers *b, const MpmReducedGrid *g, void *stream);
+
+/* The sample points' gather, g2p_sample (mpm_utils.py:415-471; defined but
+ * never launched by the reference): for sample s, particle p =
+ * sample_index[s] takes v = sum w v_out, x += dt v, F_trial = (I + dt grad v) F,
+ * F = return map(F_trial), u = x - x_initial and F_disp = F - I (written to
+ * g->f_disp).  C and the stress are not updated.  As in the reference, the
+ * von Mises return map reads (and, with hardening, updates) yield_stress[s],
+ * the sample's position in the list, not yield_stress[p] (:464).  Duplicate
+ * indices race, as they do there. */
+int mpm_g2p_sample(MpmBuffers *b, const MpmReducedGrid *g, float dt, void *stream);
+
 /* ---- element kernels on plain arrays --------------------------------- */
 
 /* Batched 3x3 SVD, A (n,9) row-major -> U (n,9), s (n,3), V (n,9):
@@ -404,8 +464,8 @@ int mpm_return_map_vjp(const MpmScene *scene, const float *F_trial, const float 
 
 /* ---- misc ------------------------------------------------------------ */
 int mpm_abi_version(void);
-/* sizeof of the ABI structs, for binding checks: out[0..3] =
- * MpmCollider, MpmScene, MpmPlan, MpmBuffers. */
+/* sizeof of the ABI structs, for binding checks: out[0..4] =
+ * MpmCollider, MpmScene, MpmPlan, MpmBuffers, MpmReducedGrid. */
 void mpm_struct_sizes(int64_t *out);
 const char *mpm_error_string(int code);
 /* Last CUDA error text seen by the library on this host thread ("" if none). */

@@ -170,3 +170,54 @@ def p2g2p(state: dict, n_grid: int, dx: float, dt: float, material: int, mu: flo
         state["yield"] = ys
     state["u"] = xn - state["x0"]
     return gm.reshape(n, n, n), gp.reshape(n, n, n, 3), gv.reshape(n, n, n, 3)
+
+
+def p2g2p_reduced(state: dict, n_grid: int, dx: float, dt: float, material: int, mu: float, lam: float,
+                  gravity, sample, density):
+    """The reduced sampled-quadrature substep without colliders, float64
+    (mpm_solver_warp.py:214-227; mpm_utils.py:318-335, :353-413).  Sets
+    state["F"] = F_disp + I on the marked particles; returns (marks, m, v_in, v_out)."""
+    inv_dx = 1.0 / dx
+    n = n_grid
+    x = state["x0"] + state["u"]
+    base, fx, w, dw = _stencil(x, inv_dx)
+    mask = np.zeros((n, n, n), np.int32)
+    offs = np.arange(-2, 3)
+    for p in np.asarray(sample):
+        b = base[p]
+        ix, iy, iz = (b[d] + offs for d in range(3))
+        ix, iy, iz = ix[(ix >= 0) & (ix < n)], iy[(iy >= 0) & (iy < n)], iz[(iz >= 0) & (iz < n)]
+        mask[np.ix_(ix, iy, iz)] = 1
+    sel = mask[base[:, 0], base[:, 1], base[:, 2]] > 0
+    F = state["F"].reshape(-1, 3, 3)
+    F[sel] = state["F_disp"].reshape(-1, 3, 3)[sel] + np.eye(3)[None]
+    Fs = F[sel]
+    U, s, V = svd_rot(Fs)
+    if material == 2:
+        ls = np.log(s).sum(1, keepdims=True)
+        c = (2.0 * mu * np.log(s) + lam * ls) / s
+        tau = np.einsum("nij,nkj->nik", _udvt(U, c, V), Fs)
+    else:
+        J = np.prod(s, axis=1)
+        R = np.einsum("nij,nkj->nik", U, V)
+        tau = 2.0 * mu * np.einsum("nij,nkj->nik", Fs - R, Fs) + (lam * J * (J - 1.0))[:, None, None] * np.eye(3)
+    m = state["mass"][sel]
+    tau = -(m / np.asarray(density)[sel])[:, None, None] * tau
+    v = state["v"][sel]
+    b, fxs, ws, dws = base[sel], fx[sel], w[sel], dw[sel]
+    gm = np.zeros(n ** 3)
+    gp = np.zeros((n ** 3, 3))
+    for i in range(3):
+        for j in range(3):
+            for k in range(3):
+                wt = ws[:, 0, i] * ws[:, 1, j] * ws[:, 2, k]
+                dwt = np.stack([dws[:, 0, i] * ws[:, 1, j] * ws[:, 2, k],
+                                ws[:, 0, i] * dws[:, 1, j] * ws[:, 2, k],
+                                ws[:, 0, i] * ws[:, 1, j] * dws[:, 2, k]], axis=1) * inv_dx
+                idx = ((b[:, 0] + i) * n + b[:, 1] + j) * n + b[:, 2] + k
+                np.add.at(gp, idx, (wt * m)[:, None] * v + dt * np.einsum("nij,nj->ni", tau, dwt))
+                np.add.at(gm, idx, wt * m)
+    gv = np.zeros_like(gp)
+    act = (mask.ravel() > 0) & (gm > 1e-10)
+    gv[act] = gp[act] / gm[act, None] + dt * np.asarray(gravity)[None]
+    return mask, gm.reshape(n, n, n), gp.reshape(n, n, n, 3), gv.reshape(n, n, n, 3)

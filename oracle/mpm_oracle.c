@@ -21,6 +21,12 @@
  *   engine_stress/mpm_solver_warp.py:429-449  surface collider kernel
  *   engine_stress/mpm_solver_warp.py:505-523  bounding-box kernel
  *   engine_stress/mpm_solver_warp.py:156-199  p2g2p launch order
+ *   engine_stress/mpm_utils.py:318-471  reduced sampled-quadrature kernels
+ *                                       (update_neighboring_cells[_for_grid_v],
+ *                                       p2g_sample_all,
+ *                                       grid_normalization_and_gravity_sample_all,
+ *                                       g2p_sample)
+ *   engine_stress/mpm_solver_warp.py:214-227  p2g2p_reduced launch order
  *
  * The 3x3 SVD (Warp's wp.svd3, third-party, unpinned version, source not in
  * the reference tree) is restated from the published method it follows:
@@ -81,6 +87,7 @@ typedef float real;
 #define ST_OUT_OF_DOMAIN 1
 #define ST_CFL 2
 #define ST_NONFINITE 4
+#define ST_BAD_INPUT 16
 
 /* Model parameters in double; every use rounds to `real` first, as Warp
  * stores them as float32 struct members (engine_stress/warp_utils.py:61-81). */
@@ -797,6 +804,207 @@ void PFX(p2g2p)(const OrcModel *m, PFX(State) * s, int64_t np, const OrcCollider
     if (status) *status |= st;
     PFX(update_u_from_x)(np, s->x, s->x0, s->u);
     PFX(update_F_disp_from_F)(np, s->F, s->F_disp);
+}
+
+/* ------------------------------------------------------------------ */
+/* reduced sampled-quadrature substep, mpm_utils.py:318-471            */
+/* ------------------------------------------------------------------ */
+
+/* update_neighboring_cells (mpm_utils.py:318-335, hi = 2) and
+ * update_neighboring_cells_for_grid_v (:338-351, hi = 4): mark the cells at
+ * offsets -2..hi of each sample point's base cell that lie inside the grid.
+ * A sample index outside [0, np) is flagged (the reference reads out of
+ * bounds); a non-finite position marks nothing and is flagged. */
+void PFX(update_neighboring_cells)(const OrcModel *m, int64_t ns, const int32_t *sample, int64_t np,
+                                   const real *x, int hi, int32_t *mask, int32_t *status) {
+    const int n = m->n_grid;
+    const real inv_dx = (real)m->inv_dx;
+    int st = 0;
+    for (int64_t s = 0; s < ns; ++s) {
+        const int64_t p = sample[s];
+        if (p < 0 || p >= np) {
+            st |= ST_BAD_INPUT;
+            continue;
+        }
+        int base[3], skip = 0;
+        for (int d = 0; d < 3; ++d) {
+            real t = x[3 * p + d] * inv_dx - (real)0.5;
+            if (!(t > (real)-8 && t < (real)(n + 8))) { /* no offset lands inside */
+                if (t != t) st |= ST_OUT_OF_DOMAIN;
+                skip = 1;
+                break;
+            }
+            base[d] = (int)t; /* wp.int truncates toward zero */
+        }
+        if (skip) continue;
+        for (int i = -2; i <= hi; ++i)
+            for (int j = -2; j <= hi; ++j)
+                for (int k = -2; k <= hi; ++k) {
+                    int ix = base[0] + i, iy = base[1] + j, iz = base[2] + k;
+                    if (0 <= ix && ix < n && 0 <= iy && iy < n && 0 <= iz && iz < n) mask[gidx(n, ix, iy, iz)] = 1;
+                }
+    }
+    if (status) *status |= st;
+}
+
+/* p2g_sample_all (mpm_utils.py:353-402), sequential scatter in particle
+ * order.  A particle whose base cell is marked sets F = F_disp + I, takes the
+ * FCR (jelly, metal) or Drucker-Prager (sand) stress of that F with
+ * J = s0 s1 s2, and scatters momentum w m v, mass w m and the force
+ * dt (-(m / density) stress grad w) as three separate adds per node.  A
+ * base cell outside the grid (the reference reads the mark array out of
+ * bounds) or a marked particle whose stencil leaves the grid is skipped and
+ * flagged. */
+void PFX(p2g_sample_all)(const OrcModel *m, int64_t np, const real *x, const real *v, real *F,
+                         const real *F_disp, const real *mass, const real *density, const int32_t *mask,
+                         real dt, real *gm, real *gvin, int32_t *status) {
+    const int n = m->n_grid;
+    const real inv_dx = (real)m->inv_dx, mu = (real)m->mu, lam = (real)m->lam;
+    int st = 0;
+    for (int64_t p = 0; p < np; ++p) {
+        int cb[3], cell_in = 1;
+        for (int d = 0; d < 3; ++d) {
+            real t = x[3 * p + d] * inv_dx - (real)0.5;
+            if (!(t > (real)-1 && t < (real)n)) cell_in = 0;
+            else cb[d] = (int)t;
+        }
+        if (!cell_in) {
+            st |= ST_OUT_OF_DOMAIN;
+            continue;
+        }
+        if (mask[gidx(n, cb[0], cb[1], cb[2])] <= 0) continue;
+        int base[3];
+        real fx[3], w[3][3], dw[3][3];
+        if (stencil(x + 3 * p, inv_dx, n, base, fx, w, dw)) {
+            st |= ST_OUT_OF_DOMAIN;
+            continue;
+        }
+        real *Fp = F + 9 * p;
+        for (int k = 0; k < 9; ++k) Fp[k] = F_disp[9 * p + k] + ((k % 4 == 0) ? (real)1 : (real)0);
+        real U[9], V[9], sig[3], tau[9];
+        PFX(svd3)(Fp, U, sig, V);
+        real J = 1;
+        for (int d = 0; d < 3; ++d) J = J * sig[d];
+        memset(tau, 0, sizeof(tau));
+        if (m->material == 0 || m->material == 1) kirchoff_stress_FCR(Fp, U, V, J, mu, lam, tau);
+        else if (m->material == 2) kirchoff_stress_drucker_prager(Fp, U, V, sig, mu, lam, tau);
+        const real mp = mass[p];
+        const real a = -(mp / density[p]);
+        real M[9];
+        for (int k = 0; k < 9; ++k) M[k] = a * tau[k];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) {
+                    real weight = w[0][i] * w[1][j] * w[2][k];
+                    int64_t g = gidx(n, base[0] + i, base[1] + j, base[2] + k);
+                    real wm = weight * mp;
+                    for (int r = 0; r < 3; ++r) gvin[3 * g + r] += wm * v[3 * p + r];
+                    gm[g] += weight * mp;
+                    real dweight[3] = {dw[0][i] * w[1][j] * w[2][k] * inv_dx,
+                                       w[0][i] * dw[1][j] * w[2][k] * inv_dx,
+                                       w[0][i] * w[1][j] * dw[2][k] * inv_dx};
+                    for (int r = 0; r < 3; ++r) {
+                        real f = M[r * 3 + 0] * dweight[0];
+                        f = f + M[r * 3 + 1] * dweight[1];
+                        f = f + M[r * 3 + 2] * dweight[2];
+                        f = f + (real)0; /* + body_force (zero) */
+                        gvin[3 * g + r] += dt * f;
+                    }
+                }
+    }
+    if (status) *status |= st;
+}
+
+/* grid_normalization_and_gravity_sample_all (mpm_utils.py:405-413): marked
+ * nodes with m > 1e-10 get v_in / m (a division) + dt g; the rest keep the
+ * zero written by zero_grid. */
+void PFX(grid_normalization_and_gravity_sample_all)(const OrcModel *m, real dt, const int32_t *mask,
+                                                    const real *gm, const real *gvin, real *gvout) {
+    const int n = m->n_grid;
+    const int64_t nn = (int64_t)n * n * n;
+    real gdt[3];
+    for (int c = 0; c < 3; ++c) gdt[c] = dt * (real)m->gravity[c];
+    for (int64_t g = 0; g < nn; ++g)
+        if (mask[g] > 0 && gm[g] > (real)1e-10f)
+            for (int c = 0; c < 3; ++c) gvout[3 * g + c] = gvin[3 * g + c] / gm[g] + gdt[c];
+}
+
+/* g2p_sample (mpm_utils.py:415-471): for sample s, particle p = sample[s]
+ * gathers v and grad v from grid_v_out, x += dt v, F_trial = (I + dt grad v) F,
+ * F = return map(F_trial) with yield_stress[s] for von Mises (the reference
+ * passes the loop index, :464), u = x - x_initial, F_disp = F - I. */
+void PFX(g2p_sample)(const OrcModel *m, int64_t ns, const int32_t *sample, int64_t np, real dt,
+                     const real *gvout, real *x, const real *x0, real *v, real *u, real *F, real *F_disp,
+                     real *yield, int32_t *status) {
+    const int n = m->n_grid;
+    const real inv_dx = (real)m->inv_dx, mu = (real)m->mu, lam = (real)m->lam;
+    int st = 0;
+    for (int64_t s = 0; s < ns; ++s) {
+        const int64_t p = sample[s];
+        if (p < 0 || p >= np || (m->material == 1 && s >= np)) {
+            st |= ST_BAD_INPUT;
+            continue;
+        }
+        int base[3];
+        real fx[3], w[3][3], dw[3][3];
+        if (stencil(x + 3 * p, inv_dx, n, base, fx, w, dw)) {
+            st |= ST_OUT_OF_DOMAIN;
+            continue;
+        }
+        real nv[3] = {0, 0, 0}, nF[9] = {0};
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) {
+                    real weight = w[0][i] * w[1][j] * w[2][k];
+                    const real *gv = gvout + 3 * gidx(n, base[0] + i, base[1] + j, base[2] + k);
+                    for (int r = 0; r < 3; ++r) nv[r] = nv[r] + gv[r] * weight;
+                    real dweight[3] = {dw[0][i] * w[1][j] * w[2][k] * inv_dx,
+                                       w[0][i] * dw[1][j] * w[2][k] * inv_dx,
+                                       w[0][i] * w[1][j] * dw[2][k] * inv_dx};
+                    for (int r = 0; r < 3; ++r)
+                        for (int c = 0; c < 3; ++c) nF[r * 3 + c] = nF[r * 3 + c] + gv[r] * dweight[c];
+                }
+        for (int r = 0; r < 3; ++r) v[3 * p + r] = nv[r];
+        for (int r = 0; r < 3; ++r) x[3 * p + r] = x[3 * p + r] + dt * nv[r];
+        real A[9], Ft[9];
+        for (int k = 0; k < 9; ++k) A[k] = ((k % 4 == 0) ? (real)1 : (real)0) + dt * nF[k];
+        mm3(A, F + 9 * p, Ft);
+        if (m->material == 1)
+            von_mises_return_mapping(Ft, mu, lam, m->hardening, (real)m->xi, yield + s, F + 9 * p);
+        else if (m->material == 2)
+            sand_return_mapping(Ft, mu, lam, (real)m->alpha, F + 9 * p);
+        else
+            memcpy(F + 9 * p, Ft, sizeof(Ft));
+        for (int k = 0; k < 9; ++k)
+            if (!isfinite(F[9 * p + k])) st |= ST_NONFINITE;
+        for (int r = 0; r < 3; ++r) u[3 * p + r] = x[3 * p + r] - x0[3 * p + r];
+        for (int k = 0; k < 9; ++k) F_disp[9 * p + k] = F[9 * p + k] - ((k % 4 == 0) ? (real)1 : (real)0);
+    }
+    if (status) *status |= st;
+}
+
+/* p2g2p_reduced in the reference's launch order (mpm_solver_warp.py:214-227):
+ * update_x_from_u, zero_grid (grids and both mark arrays), the P2G marks,
+ * p2g_sample_all, the sample-all normalization, every collider.  The caller
+ * advances moving colliders and time. */
+void PFX(p2g2p_reduced)(const OrcModel *m, PFX(State) * s, int64_t np, const real *density, int64_t ns,
+                        const int32_t *sample, int32_t *mask, int32_t *mask_v, const OrcCollider *cols,
+                        int ncol, double time, real dt, int32_t *status) {
+    const int n = m->n_grid;
+    const int64_t nn = (int64_t)n * n * n;
+    PFX(update_x_from_u)(np, s->x0, s->u, s->x);
+    PFX(zero_grid)(nn, s->grid_m, s->grid_v_in, s->grid_v_out);
+    memset(mask, 0, (size_t)nn * sizeof(int32_t));
+    memset(mask_v, 0, (size_t)nn * sizeof(int32_t));
+    PFX(update_neighboring_cells)(m, ns, sample, np, s->x, 2, mask, status);
+    PFX(p2g_sample_all)(m, np, s->x, s->v, s->F, s->F_disp, s->mass, density, mask, dt, s->grid_m,
+                        s->grid_v_in, status);
+    PFX(grid_normalization_and_gravity_sample_all)(m, dt, mask, s->grid_m, s->grid_v_in, s->grid_v_out);
+    for (int k = 0; k < ncol; ++k) {
+        if (cols[k].kind == 0) PFX(collide_surface)(m, &cols[k], time, s->grid_v_out);
+        else if (cols[k].kind == 1) PFX(collide_bounding_box)(m, &cols[k], time, s->grid_v_out);
+        else PFX(collide_extended)(m, &cols[k], time, dt, s->grid_v_out);
+    }
 }
 
 int PFX(max_threads)(void) {

@@ -22,6 +22,7 @@ from . import build as _build
 ST_OUT_OF_DOMAIN = 1
 ST_CFL = 2
 ST_NONFINITE = 4
+ST_BAD_INPUT = 16
 
 
 class OrcModel(C.Structure):
@@ -261,6 +262,11 @@ class OracleSim:
         self.grid_v_out = np.zeros((ng, ng, ng, 3), dt)
         self.time = 0.0
         self.status = C.c_int32(0)
+        # reduced sampled-quadrature state (warp_utils.py:106, :117-120; mpm_solver_warp.py:62, :81-83)
+        self.density = np.zeros(n, dt)
+        self.neighboring_cells = np.zeros((ng, ng, ng), np.int32)
+        self.neighboring_cells_grid_v = np.zeros((ng, ng, ng), np.int32)
+        self.sample_particle_index_short = np.zeros(1, np.int32)
 
     def _fn(self, name):
         return getattr(lib(self.bits), f"orc{self.bits}_{name}")
@@ -327,6 +333,42 @@ class OracleSim:
         self._fn("update_u_from_x")(C.c_int64(self.n), _ptr(self.x), _ptr(self.x0), _ptr(self.u))
         self._fn("update_F_disp_from_F")(C.c_int64(self.n), _ptr(self.F), _ptr(self.F_disp))
         self.time = self.time + dt
+
+
+    # ---- reduced sampled-quadrature substep (mpm_solver_warp.py:207-227) ----
+    def _samples(self):
+        idx = np.ascontiguousarray(self.sample_particle_index_short, dtype=np.int32).reshape(-1)
+        return idx, C.c_int64(idx.shape[0])
+
+    def p2g2p_reduced(self, dt: float) -> None:
+        """p2g2p_reduced (mpm_solver_warp.py:214-227): the grid of the sampled
+        particles' neighbourhood; particles are not moved (time += dt)."""
+        s = self._state()
+        ncol = len(self.colliders)
+        arr = (OrcCollider * max(ncol, 1))(*self.colliders)
+        idx, ns = self._samples()
+        self.density = np.ascontiguousarray(self.density, dtype=self.dtype)
+        self._fn("p2g2p_reduced")(C.byref(self.model), C.byref(s), C.c_int64(self.n), _ptr(self.density), ns,
+                                  _ptr(idx), _ptr(self.neighboring_cells), _ptr(self.neighboring_cells_grid_v),
+                                  arr, C.c_int(ncol), C.c_double(self.time), self._real(dt),
+                                  C.byref(self.status))
+        for col in self.colliders:
+            advance_collider(col, self.time, dt)
+        self.time = self.time + dt
+
+    def experiment_for_C(self) -> np.ndarray:
+        """experiment_for_C (mpm_solver_warp.py:207-209): add the -2..4 marks."""
+        idx, ns = self._samples()
+        self._fn("update_neighboring_cells")(C.byref(self.model), ns, _ptr(idx), C.c_int64(self.n), _ptr(self.x),
+                                             C.c_int(4), _ptr(self.neighboring_cells_grid_v), C.byref(self.status))
+        return self.neighboring_cells_grid_v
+
+    def g2p_sample(self, dt: float) -> None:
+        """g2p_sample (mpm_utils.py:415-471) over the sample list."""
+        idx, ns = self._samples()
+        self._fn("g2p_sample")(C.byref(self.model), ns, _ptr(idx), C.c_int64(self.n), self._real(dt),
+                               _ptr(self.grid_v_out), _ptr(self.x), _ptr(self.x0), _ptr(self.v), _ptr(self.u),
+                               _ptr(self.F), _ptr(self.F_disp), _ptr(self.yield_), C.byref(self.status))
 
 
 def svd3(A: np.ndarray, bits: int = 32):

@@ -13,7 +13,7 @@ from . import build as _build
 
 MPM_MAX_COLLIDERS = 8
 MPM_OK, MPM_ERR_ARG, MPM_ERR_CUDA, MPM_ERR_SIZE = 0, -1, -2, -3
-ST_OUT_OF_DOMAIN, ST_CFL, ST_NONFINITE, ST_INTERNAL = 1, 2, 4, 8
+ST_OUT_OF_DOMAIN, ST_CFL, ST_NONFINITE, ST_INTERNAL, ST_BAD_INPUT = 1, 2, 4, 8, 16
 JELLY, METAL, SAND = 0, 1, 2
 (COLLIDER_SURFACE, COLLIDER_BOX, COLLIDER_VPLANE, COLLIDER_CIRCLE, COLLIDER_DISK, COLLIDER_CUBE,
  COLLIDER_SPHERE) = range(7)
@@ -30,7 +30,8 @@ FIELD_COMPONENTS = {FIELD_X_INITIAL: 3, FIELD_U: 3, FIELD_V: 3, FIELD_C: 9, FIEL
 STATUS_NAMES = {ST_OUT_OF_DOMAIN: "particle stencil outside the grid (particle frozen)",
                 ST_CFL: "CFL violated: |v| > dx/dt",
                 ST_NONFINITE: "non-finite F or stress",
-                ST_INTERNAL: "particle outside its sorted block"}
+                ST_INTERNAL: "particle outside its sorted block",
+                ST_BAD_INPUT: "reduced substep: sample index outside [0, n) or grid size mismatch"}
 
 
 class MpmCollider(C.Structure):
@@ -63,6 +64,13 @@ class MpmBuffers(C.Structure):
                 ("status", C.c_void_p), ("plan", MpmPlan), ("cur", C.c_int32),
                 ("keys_valid", C.c_int32), ("collider_flags", C.c_int32), ("pad0", C.c_int32),
                 ("substep", C.c_int64)]
+
+
+class MpmReducedGrid(C.Structure):
+    _fields_ = [("sample_index", C.c_void_p), ("n_samples", C.c_int64), ("f_disp", C.c_void_p),
+                ("density", C.c_void_p), ("grid_acc", C.c_void_p), ("grid_m", C.c_void_p),
+                ("grid_v_in", C.c_void_p), ("grid_v_out", C.c_void_p), ("neighboring_cells", C.c_void_p),
+                ("neighboring_cells_grid_v", C.c_void_p), ("n_grid", C.c_int32), ("pad0", C.c_int32)]
 
 
 class MpmSurrogateConfig(C.Structure):
@@ -102,6 +110,10 @@ _SIGS = {
     "mpm_g2p": ([C.POINTER(MpmBuffers), C.c_float, C.c_void_p], C.c_int),
     "mpm_export_grid": ([C.POINTER(MpmBuffers), C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                          C.c_void_p], C.c_int),
+    "mpm_p2g2p_reduced": ([C.POINTER(MpmBuffers), C.POINTER(MpmReducedGrid), C.c_float, C.c_float, C.c_void_p],
+                          C.c_int),
+    "mpm_mark_neighboring_cells_grid_v": ([C.POINTER(MpmBuffers), C.POINTER(MpmReducedGrid), C.c_void_p], C.c_int),
+    "mpm_g2p_sample": ([C.POINTER(MpmBuffers), C.POINTER(MpmReducedGrid), C.c_float, C.c_void_p], C.c_int),
     "mpm_svd3": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
     "mpm_return_map": ([C.POINTER(MpmScene), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                         C.c_int64, C.c_void_p], C.c_int),
@@ -163,9 +175,10 @@ def load(build_if_missing: bool = False) -> C.CDLL:
 
 
 def check_abi(lib: C.CDLL) -> None:
-    out = (C.c_int64 * 4)()
+    out = (C.c_int64 * 5)()
     lib.mpm_struct_sizes(out)
-    mine = [C.sizeof(MpmCollider), C.sizeof(MpmScene), C.sizeof(MpmPlan), C.sizeof(MpmBuffers)]
+    mine = [C.sizeof(MpmCollider), C.sizeof(MpmScene), C.sizeof(MpmPlan), C.sizeof(MpmBuffers),
+            C.sizeof(MpmReducedGrid)]
     if list(out) != mine:
         raise ImportError(f"libmpm_gb300 ABI mismatch: library {list(out)} vs binding {mine}")
 

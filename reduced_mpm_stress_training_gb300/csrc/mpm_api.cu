@@ -154,6 +154,7 @@ void mpm_struct_sizes(int64_t *out) {
     out[1] = sizeof(MpmScene);
     out[2] = sizeof(MpmPlan);
     out[3] = sizeof(MpmBuffers);
+    out[4] = sizeof(MpmReducedGrid);
 }
 
 const char *mpm_error_string(int code) {
@@ -514,6 +515,41 @@ int mpm_return_map_vjp(const MpmScene *scene, const float *F_trial, const float 
     if (scene->material != MPM_SAND) return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_return_map_vjp(*scene, F_trial, F_bar, stress_bar, F_trial_bar, theta_bar, n,
                                          static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
+static int reduced_args_ok(const MpmBuffers *b, const MpmReducedGrid *g) {
+    if (!buffers_ok(b) || !g || b->plan.n_scenes != 1) return MPM_ERR_ARG;
+    if (g->n_samples < 0 || (g->n_samples > 0 && !g->sample_index) || g->n_grid < 1) return MPM_ERR_ARG;
+    if (!g->f_disp || !g->density || !g->grid_acc || !g->grid_m || !g->grid_v_in || !g->grid_v_out ||
+        !g->neighboring_cells || !g->neighboring_cells_grid_v)
+        return MPM_ERR_ARG;
+    if (g->n_samples > ((int64_t)1 << 26) || g->n_grid > 2048) return MPM_ERR_SIZE;
+    return MPM_OK;
+}
+
+int mpm_p2g2p_reduced(MpmBuffers *b, const MpmReducedGrid *g, float time, float dt, void *stream) {
+    int r = reduced_args_ok(b, g);
+    if (r) return r;
+    MPM_CHECK(mpm::launch_p2g2p_reduced(make_ctx(b, stream, b->cur), *g, time, dt));
+    if (b->collider_flags & MPM_CF_MOVING)  // the reference's modify_bc after each collider sweep
+        MPM_CHECK(mpm::launch_advance_colliders(static_cast<MpmScene *>(b->scenes), b->plan.n_scenes, time, dt,
+                                                static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
+int mpm_mark_neighboring_cells_grid_v(MpmBuffers *b, const MpmReducedGrid *g, void *stream) {
+    int r = reduced_args_ok(b, g);
+    if (r) return r;
+    MPM_CHECK(mpm::launch_mark_grid_v(make_ctx(b, stream, b->cur), *g));
+    return MPM_OK;
+}
+
+int mpm_g2p_sample(MpmBuffers *b, const MpmReducedGrid *g, float dt, void *stream) {
+    int r = reduced_args_ok(b, g);
+    if (r) return r;
+    MPM_CHECK(mpm::launch_g2p_sample(make_ctx(b, stream, b->cur), *g, dt));
+    b->keys_valid = 0;  // the sample points moved
     return MPM_OK;
 }
 

@@ -608,4 +608,111 @@ __device__ __forceinline__ void return_map_stress(const MpmScene &S, const float
     }
 }
 
+// ---------------------------------------------------------------------------
+// Colliders: the reference's grid_postprocess kernels
+// (engine_stress/mpm_solver_warp.py:407-720), one per collider kind, applied
+// in registration order to the node velocity after normalization + gravity.
+// The reference sweeps the dense grid; in the substep, nodes outside the
+// active blocks carry no mass and are never gathered, so the active blocks are
+// enough (the reduced substep sweeps its dense grid as the reference does).  Node
+// offsets and dot products use explicitly rounded float32 operations (no FMA
+// contraction) so inside/outside decisions match a float32 restatement.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float dot3_rn(float a0, float a1, float a2, const float b[3]) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a0, b[0]), __fmul_rn(a1, b[1])), __fmul_rn(a2, b[2]));
+}
+
+// rotation angle of the circling column's centre about (0.5, *, 0.5), from
+// its bottom point (set_column_moving_as_circle, :585-592 and :597-603)
+__device__ __forceinline__ float circle_theta(const float p[3]) {
+    const float z0 = __fsub_rn(p[0], 0.5f), z1 = p[1], z2 = __fsub_rn(p[2], 0.5f);
+    const float len = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(z0, z0), __fmul_rn(z1, z1)), __fmul_rn(z2, z2)));
+    const float c = __fdiv_rn(z0, len);
+    const float th = acosf(fminf(fmaxf(c, -1.0f), 1.0f));
+    return z2 < 0.0f ? -th : th;
+}
+
+__device__ __forceinline__ void apply_collider(const MpmCollider &cl, const MpmScene &S, int ix, int iy, int iz,
+                                               float time, float dt, float v[3]) {
+    const bool active = time >= cl.start_time && time < cl.end_time;
+    const float o0 = __fsub_rn(__fmul_rn((float)ix, S.dx), cl.point[0]);
+    const float o1 = __fsub_rn(__fmul_rn((float)iy, S.dx), cl.point[1]);
+    const float o2 = __fsub_rn(__fmul_rn((float)iz, S.dx), cl.point[2]);
+    switch (cl.kind) {
+        case MPM_COLLIDER_SURFACE:  // :429-449: every surface type writes zero
+            if (active && dot3_rn(o0, o1, o2, cl.normal) < 0.0f) v[0] = v[1] = v[2] = 0.0f;
+            break;
+        case MPM_COLLIDER_BOX: {  // :505-523, padding 3
+            if (!active) break;
+            const int id[3] = {ix, iy, iz};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (id[d] < 3 && v[d] < 0.0f) v[d] = 0.0f;
+                if (id[d] >= S.n_grid - 3 && v[d] > 0.0f) v[d] = 0.0f;
+            }
+            break;
+        }
+        case MPM_COLLIDER_VPLANE: {  // :545-559: the slab |(x - p).n| <= threshold moves with velocity
+            const bool in = fabsf(dot3_rn(o0, o1, o2, cl.normal)) <= cl.threshold;
+            if (active) {
+                if (in) v[0] = cl.velocity[0], v[1] = cl.velocity[1], v[2] = cl.velocity[2];
+            } else if (cl.reset == 1 && time < __fadd_rn(cl.end_time, __fmul_rn(__fmul_rn(1.5f, dt), 10.0f))) {
+                if (in) v[0] = v[1] = v[2] = 0.0f;
+            }
+            break;
+        }
+        case MPM_COLLIDER_CIRCLE: {  // :580-592: a vertical column circling about (0.5, *, 0.5)
+            if (!active) break;
+            if (__fadd_rn(__fmul_rn(o0, o0), __fmul_rn(o2, o2)) < __fmul_rn(cl.radius, cl.radius) &&
+                fabsf(o1) < cl.height) {
+                const float th = circle_theta(cl.point);
+                v[0] = -cl.v_scale * sinf(th);
+                v[1] = 0.0f;
+                v[2] = cl.v_scale * cosf(th);
+            }
+            break;
+        }
+        case MPM_COLLIDER_DISK: {  // :635-659: rigid rotation of a disk about its normal
+            if (active) {
+                if (fabsf(dot3_rn(o0, o1, o2, cl.normal)) < cl.width) {
+                    // the reference takes r = (0, o_y, o_z), not the in-plane projection
+                    const float rl = sqrtf(__fadd_rn(__fmul_rn(o1, o1), __fmul_rn(o2, o2)));
+                    if (rl < cl.radius) {
+                        if (rl > 0.0f) {  // on the axis the reference divides 0 by 0 (NaN); here v = 0
+                            const float c = __fdiv_rn(dot3_rn(0.0f, o1, o2, cl.x_unit), rl);
+                            float th = acosf(fminf(fmaxf(c, -1.0f), 1.0f));
+                            if (dot3_rn(0.0f, o1, o2, cl.y_unit) < 0.0f) th = -th;
+                            const float sx = -rl * sinf(th) * cl.v_scale, sy = rl * cosf(th) * cl.v_scale;
+#pragma unroll
+                            for (int d = 0; d < 3; ++d) v[d] = sx * cl.x_unit[d] + sy * cl.y_unit[d];
+                        } else {
+                            v[0] = v[1] = v[2] = 0.0f;
+                        }
+                    }
+                }
+            } else if (cl.reset == 1 && time < __fadd_rn(cl.end_time, __fmul_rn(1.5f, dt))) {
+                v[0] = v[1] = v[2] = 0.0f;  // every node, as the reference does
+            }
+            break;
+        }
+        case MPM_COLLIDER_CUBE: {  // :680-689
+            if (active) {
+                if (fabsf(o0) < cl.width && fabsf(o1) < cl.width && fabsf(o2) < cl.width)
+                    v[0] = cl.velocity[0], v[1] = cl.velocity[1], v[2] = cl.velocity[2];
+            } else if (cl.reset == 1 && time < __fadd_rn(cl.end_time, __fmul_rn(1.5f, dt))) {
+                v[0] = v[1] = v[2] = 0.0f;  // every node, as the reference does
+            }
+            break;
+        }
+        case MPM_COLLIDER_SPHERE: {  // :709-714
+            if (!active) break;
+            const float len = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(o0, o0), __fmul_rn(o1, o1)), __fmul_rn(o2, o2)));
+            if (len < cl.radius) v[0] = cl.velocity[0], v[1] = cl.velocity[1], v[2] = cl.velocity[2];
+            break;
+        }
+        default:
+            break;
+    }
+}
+
 }  // namespace mpm

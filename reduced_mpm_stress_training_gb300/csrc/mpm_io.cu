@@ -78,6 +78,12 @@ __global__ void slot_of_uid_kernel(PState st, int n, int *__restrict__ inv) {
     inv[__float_as_int(ldrec(st, i, 1).y)] = i;
 }
 
+cudaError_t launch_slot_of_uid(const Ctx &cx) {
+    if (cx.n == 0) return cudaSuccess;
+    slot_of_uid_kernel<<<(unsigned)((cx.n + 255) / 256), 256, 0, cx.stream>>>(cx.st, cx.n, cx.ws.slot_of_uid);
+    return cudaGetLastError();
+}
+
 // load_uvstress_from_tensor (mpm_solver_warp.py:253-266) in one pass: u, v
 // and stress of user particle `id` into its record (quads 2, 3, 5-7; the C
 // words sharing quads 3 and 5 are kept)

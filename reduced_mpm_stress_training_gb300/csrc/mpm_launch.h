@@ -71,6 +71,14 @@ cudaError_t launch_svd3(const float *A, float *U, float *s, float *V, int64_t n,
 cudaError_t launch_return_map(const MpmScene &scene, const float *Ft, float *yld, float *F,
                               float *tau, int64_t n, cudaStream_t st);
 
+// slot_of_uid[uid] = slot of the live state (mpm_io.cu)
+cudaError_t launch_slot_of_uid(const Ctx &cx);
+
+// reduced sampled-quadrature substep (mpm_reduced.cu); see mpm_p2g2p_reduced
+cudaError_t launch_p2g2p_reduced(const Ctx &cx, const MpmReducedGrid &g, float time, float dt);
+cudaError_t launch_mark_grid_v(const Ctx &cx, const MpmReducedGrid &g);
+cudaError_t launch_g2p_sample(const Ctx &cx, const MpmReducedGrid &g, float dt);
+
 int field_components(int field);
 
 }  // namespace mpm

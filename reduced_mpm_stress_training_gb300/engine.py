@@ -430,6 +430,37 @@ class MPMEngine:
         else:
             raise ValueError(name)
 
+    # ------------------------------------------------------------------ reduced substep
+    def _single_scene(self, what: str) -> None:
+        if len(self.scenes) != 1:
+            raise ValueError(f"{what} serves single-scene engines")
+
+    def p2g2p_reduced(self, grid: "ReducedGrid", time: float, dt: float) -> None:
+        """The reduced sampled-quadrature substep into ``grid`` (mpm_p2g2p_reduced)."""
+        self._single_scene("p2g2p_reduced")
+        g = grid.struct(self)
+        self.poll_status()
+        A.check(self.lib.mpm_p2g2p_reduced(C.byref(self.buf), C.byref(g), time, dt, self.stream),
+                "mpm_p2g2p_reduced")
+        self._queue_status()
+
+    def mark_neighboring_cells_grid_v(self, grid: "ReducedGrid") -> None:
+        """Add the -2..4 marks of the sample points (mpm_mark_neighboring_cells_grid_v)."""
+        self._single_scene("experiment_for_C")
+        g = grid.struct(self)
+        self.poll_status()
+        A.check(self.lib.mpm_mark_neighboring_cells_grid_v(C.byref(self.buf), C.byref(g), self.stream),
+                "mpm_mark_neighboring_cells_grid_v")
+        self._queue_status()
+
+    def g2p_sample(self, grid: "ReducedGrid", dt: float) -> None:
+        """The sample points' gather from grid.grid_v_out (mpm_g2p_sample)."""
+        self._single_scene("g2p_sample")
+        g = grid.struct(self)
+        self.poll_status()
+        A.check(self.lib.mpm_g2p_sample(C.byref(self.buf), C.byref(g), dt, self.stream), "mpm_g2p_sample")
+        self._queue_status()
+
     # ------------------------------------------------------------------ checkpoints
     def reinit(self) -> None:
         """Back to the freshly initialised state (mpm_init: zero state, F = I,
@@ -482,6 +513,58 @@ class MPMEngine:
     def clear_status(self) -> None:
         self._status.zero_()
         self._pending = False
+
+
+class ReducedGrid:
+    """Buffers of the reduced sampled-quadrature substep (MpmReducedGrid).
+
+    The dense (n, n, n) grids of the reference's state -- grid_m, grid_v_in,
+    grid_v_out and the int32 marks neighboring_cells / neighboring_cells_grid_v
+    (engine_stress/warp_utils.py:109-120) -- plus a float4 accumulation
+    scratch; and, set by the caller before each call, the user-order sample
+    list (int32), F_disp (n, 3, 3) and density (n) the kernels read.
+    """
+
+    def __init__(self, n_grid: int, device):
+        ng = int(n_grid)
+        dev = torch.device(device)
+        f32 = torch.float32
+        self.n_grid = ng
+        self.grid_m = torch.zeros((ng, ng, ng), dtype=f32, device=dev)
+        self.grid_v_in = torch.zeros((ng, ng, ng, 3), dtype=f32, device=dev)
+        self.grid_v_out = torch.zeros((ng, ng, ng, 3), dtype=f32, device=dev)
+        self.neighboring_cells = torch.zeros((ng, ng, ng), dtype=torch.int32, device=dev)
+        self.neighboring_cells_grid_v = torch.zeros((ng, ng, ng), dtype=torch.int32, device=dev)
+        self.grid_acc = torch.zeros((ng ** 3, 4), dtype=f32, device=dev)
+        self.sample_index: torch.Tensor | None = None
+        self.f_disp: torch.Tensor | None = None
+        self.density: torch.Tensor | None = None
+
+    def struct(self, engine: MPMEngine) -> A.MpmReducedGrid:
+        n = engine.n_particles
+        dev = engine.device
+        checks = ((self.sample_index, torch.int32, None), (self.f_disp, torch.float32, n * 9),
+                  (self.density, torch.float32, n))
+        for t, dt, numel in checks:
+            if t is None or t.device != dev or t.dtype != dt or not t.is_contiguous() or \
+                    (numel is not None and t.numel() != numel):
+                raise ValueError("reduced substep: sample_index (int32), f_disp (n x 9) and density (n) "
+                                 "must be contiguous tensors on the engine's device")
+        if engine.scenes[0].n_grid != self.n_grid:
+            raise ValueError("reduced substep: the grid was sized for another n_grid")
+        g = A.MpmReducedGrid()
+        g.sample_index = self.sample_index.data_ptr()
+        g.n_samples = self.sample_index.numel()
+        g.f_disp = self.f_disp.data_ptr()
+        g.density = self.density.data_ptr()
+        g.grid_acc = self.grid_acc.data_ptr()
+        g.grid_m = self.grid_m.data_ptr()
+        g.grid_v_in = self.grid_v_in.data_ptr()
+        g.grid_v_out = self.grid_v_out.data_ptr()
+        g.neighboring_cells = self.neighboring_cells.data_ptr()
+        g.neighboring_cells_grid_v = self.neighboring_cells_grid_v.data_ptr()
+        g.n_grid = self.n_grid
+        return g
 
 
 class SubstepGraph:

@@ -23,15 +23,23 @@ the current PyTorch CUDA stream.  Differences a caller can see:
   parameters are refreshed from the device when the scene is re-uploaded.
   ``set_rotation_on_disk`` raises ValueError for |normal[0]| <= 0.1 (the
   reference's axis search loops forever there) and gives v = 0 to nodes on
-  the disk axis (the reference divides 0 by 0).  The reduced
-  sampled-quadrature substep ``p2g2p_reduced`` raises NotImplementedError.
+  the disk axis (the reference divides 0 by 0).
+* The reduced sampled-quadrature substep ``p2g2p_reduced`` (:214-227) and
+  ``experiment_for_C`` (:207-209) work on dense (n, n, n) grids as the
+  reference's do; the reference has no setter for the sample list, so
+  ``load_sample_particle_index_from_tensor`` (or assigning
+  ``mpm_state.sample_particle_index_short``) sets it, and ``g2p_sample(dt)``
+  launches the sample gather the reference defines but never calls
+  (engine_stress/mpm_utils.py:415-471).  A particle whose base cell is outside
+  the grid, or a sample index outside [0, n), sets a status bit where the
+  reference would index out of bounds.
 """
 from __future__ import annotations
 
 import torch
 
 from . import _capi as A
-from .engine import (Collider, MPMEngine, MPMStatusError, SceneParams, lame_from_E_nu,
+from .engine import (Collider, MPMEngine, MPMStatusError, ReducedGrid, SceneParams, lame_from_E_nu,
                      material_code, dp_alpha)
 
 
@@ -83,10 +91,22 @@ class _State:
             return sim._f_disp()
         if name == "particle_density":
             return sim._density
+        if name == "sample_particle_index_short":
+            return sim._sample_index
+        if name in ("neighboring_cells", "neighboring_cells_grid_v"):
+            return getattr(sim._reduced_grid(), name)
         if name in ("grid_m", "grid_v_in", "grid_v_out"):
+            if sim._grid_from_reduced:  # the dense grid of the last p2g2p_reduced
+                return getattr(sim._reduced_grid(), name)
             gm, gvin, gvout = eng.export_grid(0)
             return {"grid_m": gm, "grid_v_in": gvin, "grid_v_out": gvout}[name]
         raise AttributeError(name)
+
+    def __setattr__(self, name, value):
+        if name == "sample_particle_index_short":
+            self.__dict__["_sim"].load_sample_particle_index_from_tensor(value)
+        else:
+            super().__setattr__(name, value)
 
 
 class MPMSimulator:
@@ -110,6 +130,10 @@ class MPMSimulator:
         self.device = self._engine.device
         self._density = torch.zeros(self.n_particles, dtype=torch.float32, device=self.device)
         self._f_disp_loaded = None
+        # sample_particle_index_short starts as one zero index (mpm_solver_warp.py:83)
+        self._sample_index = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._reduced = None
+        self._grid_from_reduced = False
         self.time = 0.0
         self.mpm_model = _Model(self)
         self.mpm_state = _State(self)
@@ -229,6 +253,7 @@ class MPMSimulator:
         """One substep, engine_stress/mpm_solver_warp.py:156-203."""
         self._engine.substep(float(self.time), float(dt))
         self._f_disp_loaded = None
+        self._grid_from_reduced = False
         self.time = self.time + dt
         if print_norm:
             u, v, fd, st = self.export_uvFstress_from_warp()
@@ -299,9 +324,57 @@ class MPMSimulator:
         """engine_stress/mpm_solver_warp.py:697-720"""
         self._add_collider(Collider.sphere(center, radius, velocity, start_time, end_time))
 
-    def p2g2p_reduced(self, *a, **k):
-        raise NotImplementedError("the reduced sampled-quadrature substep is outside the GB300 "
-                                  "substep's scope")
+    # --------------------------------------------------------------- reduced substep
+    def load_sample_particle_index_from_tensor(self, tensor_index):
+        """Extension: the sample list (sample_particle_index_short, warp_utils.py:120),
+        user particle indices."""
+        t = torch.as_tensor(tensor_index).detach().reshape(-1)
+        if t.dtype.is_floating_point or t.dtype == torch.bool:
+            raise TypeError("sample indices must be integers")
+        self._sample_index = t.to(device=self.device, dtype=torch.int32).contiguous()
+
+    def _reduced_grid(self) -> ReducedGrid:
+        ng = self._params.n_grid
+        if self._reduced is None or self._reduced.n_grid != ng:
+            self._reduced = ReducedGrid(ng, self.device)
+        rg = self._reduced
+        rg.sample_index = self._sample_index
+        rg.density = self._density.contiguous()
+        return rg
+
+    def _f_disp_state(self) -> torch.Tensor:
+        """particle_F_disp as its own array: F - I after a substep, the loaded
+        tensor after load_uvF_from_tensor; the reduced kernels read and write it."""
+        if self._f_disp_loaded is None:
+            self._f_disp_loaded = self._engine.export(A.FIELD_F_DISP).reshape(self.n_particles, 3, 3)
+        return self._f_disp_loaded
+
+    def p2g2p_reduced(self, step, dt, device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:214-227: the grid of the sample points'
+        neighbourhood (mpm_state.grid_m / grid_v_in / grid_v_out); particles whose
+        base cell is marked set F = F_disp + I; nothing moves; time += dt."""
+        rg = self._reduced_grid()
+        rg.f_disp = self._f_disp_state()
+        self._engine.p2g2p_reduced(rg, float(self.time), float(dt))
+        self._grid_from_reduced = True
+        self.time = self.time + dt
+
+    def experiment_for_C(self, device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:207-209: adds the -2..4 marks of the
+        sample points and returns neighboring_cells_grid_v (the live array)."""
+        rg = self._reduced_grid()
+        rg.f_disp = self._f_disp_state()
+        self._engine.mark_neighboring_cells_grid_v(rg)
+        return rg.neighboring_cells_grid_v
+
+    def g2p_sample(self, dt, device="cuda:0"):
+        """Extension: launch g2p_sample (engine_stress/mpm_utils.py:415-471) on the
+        grid of the last p2g2p_reduced.  The sample particles take v, x, F and
+        F_disp from grid_v_out; yield_stress is read at the sample's list
+        position, as there (:464)."""
+        rg = self._reduced_grid()
+        rg.f_disp = self._f_disp_state()
+        self._engine.g2p_sample(rg, float(dt))
 
 
 MPM_Simulator_WARP = MPMSimulator
