@@ -274,7 +274,7 @@ typedef struct MpmReducedGrid {
     float *grid_v_out;           /* n^3 x 3   velocity after the colliders  */
     int32_t *neighboring_cells;        /* n^3 marks of the P2G (:318-335)    */
     int32_t *neighboring_cells_grid_v; /* n^3 marks for the gather (:338-351) */
-    int32_t n_grid;              /* n: must equal the scene's n_grid        */
+    int32_t n_grid;              /* n: the scene's n_grid, at most 1024     */
     int32_t pad0;
 } MpmReducedGrid; /* 88 bytes */
 

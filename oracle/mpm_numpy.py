@@ -6,7 +6,7 @@ are written separately -- this one vectorised over particles, with
 convention (U, V proper rotations, det sign on the last singular value) --
 and must agree to float64 rounding on small cases.
 
-Follows engine_stress/mpm_utils.py:29-112 (stress, return maps),
+Follows engine_stress/mpm_utils.py:29-112 (stress, return maps), :318-413 (reduced P2G),
 :190-237 (P2G, grid update), :241-306 (G2P) and
 engine_stress/mpm_solver_warp.py:156-199 (order), :429-449, :505-523 (BCs).
 """

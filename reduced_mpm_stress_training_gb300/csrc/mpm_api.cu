@@ -524,7 +524,7 @@ static int reduced_args_ok(const MpmBuffers *b, const MpmReducedGrid *g) {
     if (!g->f_disp || !g->density || !g->grid_acc || !g->grid_m || !g->grid_v_in || !g->grid_v_out ||
         !g->neighboring_cells || !g->neighboring_cells_grid_v)
         return MPM_ERR_ARG;
-    if (g->n_samples > ((int64_t)1 << 26) || g->n_grid > 2048) return MPM_ERR_SIZE;
+    if (g->n_samples > ((int64_t)1 << 26) || g->n_grid > 1024) return MPM_ERR_SIZE;
     return MPM_OK;
 }
 

@@ -117,61 +117,89 @@ __global__ void __launch_bounds__(256) mark_kernel(const MpmScene *__restrict__ 
 // particle whose base cell is marked sets F = F_disp + I, takes the stress of
 // that F (FCR for jelly and metal, Drucker-Prager for sand; :368-378) and
 // scatters, per node, w m v + dt (-(m / density) stress grad w) and w m.
+// The records are sorted by cell, so neighbouring lanes mostly share a base
+// cell and hit the same 27 nodes: each node's contributions are summed over
+// every run of lanes with one base cell (a segmented shuffle reduction) and
+// the run's first lane issues one 16-byte atomic for it.
 __global__ void __launch_bounds__(256) reduced_p2g_kernel(const MpmScene *__restrict__ scenes, PState st,
                                                           MpmReducedGrid g, int n, float dt, int *status) {
     const MpmScene &S = scenes[0];
-    if (!grid_matches(S, g, status)) return;
+    if (!grid_matches(S, g, status)) return;  // the same for every thread
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int lane = threadIdx.x & 31;
     const int N = g.n_grid;
-    float gp[3];
-    record_gp(st, i, S.inv_dx, gp);
-    int base[3];
-    bool cell_in = true, stencil_in = true;
+    float gp[3] = {0.5f, 0.5f, 0.5f};
+    int base[3] = {0, 0, 0};
+    bool act = false;
+    if (i < n) {
+        record_gp(st, i, S.inv_dx, gp);
+        bool cell_in = true, stencil_in = true;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const float t = __fsub_rn(gp[d], 0.5f);
-        cell_in = cell_in && t > -1.0f && t < (float)N;
-        stencil_in = stencil_in && t > -1.0f && t < (float)(N - 2);
-        base[d] = (t > -1.0f && t < (float)N) ? (int)t : 0;
+        for (int d = 0; d < 3; ++d) {
+            const float t = __fsub_rn(gp[d], 0.5f);
+            cell_in = cell_in && t > -1.0f && t < (float)N;
+            stencil_in = stencil_in && t > -1.0f && t < (float)(N - 2);
+            base[d] = (t > -1.0f && t < (float)N) ? (int)t : 0;
+        }
+        if (!cell_in) {  // the reference reads the mark array out of bounds here
+            atomicOr(status, MPM_ST_OUT_OF_DOMAIN);
+        } else if (g.neighboring_cells[dense_index(N, base[0], base[1], base[2])] > 0) {
+            if (stencil_in) act = true;
+            else atomicOr(status, MPM_ST_OUT_OF_DOMAIN);  // marked, but the stencil would leave the grid
+        }
     }
-    if (!cell_in) {  // the reference reads the mark array out of bounds here
-        atomicOr(status, MPM_ST_OUT_OF_DOMAIN);
-        return;
-    }
-    if (g.neighboring_cells[dense_index(N, base[0], base[1], base[2])] <= 0) return;
-    if (!stencil_in) {  // marked, but the 3x3x3 stencil would leave the grid
-        atomicOr(status, MPM_ST_OUT_OF_DOMAIN);
-        return;
-    }
-    float4 q1 = ldrec(st, i, 1);
-    const float4 q0 = ldrec(st, i, 0), q2 = ldrec(st, i, 2), q3 = ldrec(st, i, 3);
-    const int uid = __float_as_int(q1.y);
-    const float *fd = g.f_disp + (int64_t)uid * 9;
-    float F[9];
+    if (__ballot_sync(0xffffffffu, act) == 0u) return;  // the whole warp leaves together
+    float tau[9], v[3] = {0.f, 0.f, 0.f}, m = 0.0f;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) F[k] = __fadd_rn(fd[k], (k % 4 == 0) ? 1.0f : 0.0f);  // F_disp + I (:364)
-    q1.w = F[8];
-    strec(st, i, 1, q1);
-    strec(st, i, 8, make_float4(F[0], F[1], F[2], F[3]));
-    strec(st, i, 9, make_float4(F[4], F[5], F[6], F[7]));
-    Svd d;
-    svd3(F, d);
-    float tau[9];
-    if (S.material == MPM_SAND) {
-        stress_dp(F, d, S.mu, S.lam, tau);
-    } else {
-        const float J = d.s[0] * d.s[1] * d.s[2];
-        stress_fcr(F, d, J, S.mu, S.lam, tau);
-    }
-    const float m = q0.w;
-    const float nvol = -__fdiv_rn(m, g.density[uid]);  // -(m / density), :395
+    for (int k = 0; k < 9; ++k) tau[k] = 0.0f;
+    if (act) {
+        float4 q1 = ldrec(st, i, 1);
+        const float4 q0 = ldrec(st, i, 0), q2 = ldrec(st, i, 2), q3 = ldrec(st, i, 3);
+        const int uid = __float_as_int(q1.y);
+        const float *fd = g.f_disp + (int64_t)uid * 9;
+        float F[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) tau[k] *= nvol;
-    const float v[3] = {q2.w, q3.x, q3.y};
+        for (int k = 0; k < 9; ++k) F[k] = __fadd_rn(fd[k], (k % 4 == 0) ? 1.0f : 0.0f);  // F_disp + I (:364)
+        q1.w = F[8];
+        strec(st, i, 1, q1);
+        strec(st, i, 8, make_float4(F[0], F[1], F[2], F[3]));
+        strec(st, i, 9, make_float4(F[4], F[5], F[6], F[7]));
+        Svd d;
+        svd3(F, d);
+        if (S.material == MPM_SAND) {
+            stress_dp(F, d, S.mu, S.lam, tau);
+        } else {
+            const float J = d.s[0] * d.s[1] * d.s[2];
+            stress_fcr(F, d, J, S.mu, S.lam, tau);
+        }
+        m = q0.w;
+        const float nvol = -__fdiv_rn(m, g.density[uid]);  // -(m / density), :395
+#pragma unroll
+        for (int k = 0; k < 9; ++k) tau[k] *= nvol;
+        v[0] = q2.w;
+        v[1] = q3.x;
+        v[2] = q3.y;
+    } else {  // contributes zeros from a finite stencil
+        gp[0] = gp[1] = gp[2] = 0.5f;
+        base[0] = base[1] = base[2] = 0;
+    }
+    // runs of lanes with one base cell (n_grid <= 1024: 10 bits per axis); idle lanes stand alone
+    const int key = act ? ((base[0] << 20) | (base[1] << 10) | base[2]) : (0x40000000 | lane);
+    const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const bool head = lane == 0 || prev != key;
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const bool solo = heads == 0xffffffffu;  // no two lanes share a cell: plain atomics
+    // lane + 2^j belongs to this lane's run when no run starts in (lane, lane + 2^j]
+    bool in_run[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        const int d = 1 << j;
+        in_run[j] = lane + d < 32 && ((((unsigned long long)heads) >> (lane + 1)) & ((1ull << d) - 1ull)) == 0ull;
+    }
     Weights W;
     make_weights(gp, base, W);
     const float inv_dx = S.inv_dx;
+    float4 *acc = static_cast<float4 *>(g.grid_acc);
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -189,8 +217,23 @@ __global__ void __launch_bounds__(256) reduced_p2g_kernel(const MpmScene *__rest
                 add.y = wm * v[1] + dt * (tau[3] * dg[0] + tau[4] * dg[1] + tau[5] * dg[2]);
                 add.z = wm * v[2] + dt * (tau[6] * dg[0] + tau[7] * dg[1] + tau[8] * dg[2]);
                 add.w = wm;
-                atomicAdd(static_cast<float4 *>(g.grid_acc) + dense_index(N, base[0] + a, base[1] + b, base[2] + c),
-                          add);
+                if (!solo) {
+#pragma unroll
+                    for (int j = 0; j < 5; ++j) {
+                        const int d = 1 << j;
+                        const float ox = __shfl_down_sync(0xffffffffu, add.x, d);
+                        const float oy = __shfl_down_sync(0xffffffffu, add.y, d);
+                        const float oz = __shfl_down_sync(0xffffffffu, add.z, d);
+                        const float ow = __shfl_down_sync(0xffffffffu, add.w, d);
+                        if (in_run[j]) {
+                            add.x += ox;
+                            add.y += oy;
+                            add.z += oz;
+                            add.w += ow;
+                        }
+                    }
+                }
+                if (act && head) atomicAdd(acc + dense_index(N, base[0] + a, base[1] + b, base[2] + c), add);
             }
         }
 }
