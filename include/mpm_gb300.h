@@ -310,6 +310,43 @@ int mpm_mark_neighboring_cells_grid_v(MpmBuffers *b, const MpmReducedGrid *g, vo
  * indices race, as they do there. */
 int mpm_g2p_sample(MpmBuffers *b, const MpmReducedGrid *g, float dt, void *stream);
 
+/* ---- the reference's stress decoder in the loop ------------------------
+ * NetDec (offline_training_xhat_and_stress_and_mu/CROMnet_secondary.py:203-301,
+ * with Prepare :487-525, Activation :447-463 and invStandardizeQ :465-477):
+ * rows (label, x, mu) -> Prepare(x) -> 5 x [Linear(hidden), activation] ->
+ * Linear(6) -> mean_q + q * std_q, the six stress components
+ * [xx, xy, xz, yy, yz, zz] (mpm_solver_warp.py:383).  FP32. */
+typedef struct MpmStressDecoder {
+    const float *params; /* device, packed float32, PyTorch [out, in] weights:
+                            dec0.weight (hidden x in), dec0.bias (hidden),
+                            dec1..dec4 weights (hidden x hidden each), their biases
+                            (hidden each), enc.weight (6 x hidden), enc.bias (6),
+                            prepare (6: min_x, max_x with SIREN, else mean_x, std_x),
+                            mean_q (6), std_q (6); in = label_dim + 3 + mu_dim      */
+    int32_t label_dim;   /* lbllength, 0..64                                       */
+    int32_t mu_dim;      /* 0..4 (the reference's data: 1, the friction angle)     */
+    int32_t hidden;      /* i_dim * scale_mlp, 1..64 (the reference's default: 30)  */
+    int32_t siren;       /* 1: sin(omega_0 x) and clip-to-[-1, 1]; 0: ELU, standardise */
+    float omega_0;
+    int32_t pad0;
+} MpmStressDecoder; /* 32 bytes */
+
+/* Number of floats of the packed parameter blob (negative: bad dimensions). */
+int64_t mpm_decoder_param_count(const MpmStressDecoder *d);
+
+/* NetDec.forward (CROMnet_secondary.py:288-291) on n device rows of
+ * label_dim + 3 + mu_dim floats -> out (n, 6). */
+int mpm_decoder_forward(const MpmStressDecoder *d, const float *rows, float *out, int64_t n, void *stream);
+
+/* The decoder as the stress source of the next substep (the reduced-order loop
+ * feeds it through load_uvstress_from_tensor, mpm_solver_warp.py:253-266):
+ * every particle's row is (label, its x_initial, its mu row), label one
+ * frame's label_dim floats and mu (n, mu_dim) in user order (NULL when
+ * mu_dim = 0); the decoded components are written as the symmetric stress
+ * [q0 q1 q2; q1 q3 q4; q2 q4 q5] of the particle, read by the next mpm_p2g2p. */
+int mpm_decoder_stress(MpmBuffers *b, const MpmStressDecoder *d, const float *label, const float *mu,
+                       void *stream);
+
 /* ---- element kernels on plain arrays --------------------------------- */
 
 /* Batched 3x3 SVD, A (n,9) row-major -> U (n,9), s (n,3), V (n,9):
@@ -464,8 +501,8 @@ int mpm_return_map_vjp(const MpmScene *scene, const float *F_trial, const float 
 
 /* ---- misc ------------------------------------------------------------ */
 int mpm_abi_version(void);
-/* sizeof of the ABI structs, for binding checks: out[0..4] =
- * MpmCollider, MpmScene, MpmPlan, MpmBuffers, MpmReducedGrid. */
+/* sizeof of the ABI structs, for binding checks: out[0..5] =
+ * MpmCollider, MpmScene, MpmPlan, MpmBuffers, MpmReducedGrid, MpmStressDecoder. */
 void mpm_struct_sizes(int64_t *out);
 const char *mpm_error_string(int code);
 /* Last CUDA error text seen by the library on this host thread ("" if none). */

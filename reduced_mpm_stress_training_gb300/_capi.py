@@ -73,6 +73,11 @@ class MpmReducedGrid(C.Structure):
                 ("neighboring_cells_grid_v", C.c_void_p), ("n_grid", C.c_int32), ("pad0", C.c_int32)]
 
 
+class MpmStressDecoder(C.Structure):
+    _fields_ = [("params", C.c_void_p), ("label_dim", C.c_int32), ("mu_dim", C.c_int32),
+                ("hidden", C.c_int32), ("siren", C.c_int32), ("omega_0", C.c_float), ("pad0", C.c_int32)]
+
+
 class MpmSurrogateConfig(C.Structure):
     _fields_ = [("tol", C.c_float), ("rho_min", C.c_float), ("rho_max", C.c_float),
                 ("nu_min", C.c_float), ("nu_max", C.c_float), ("phi_min", C.c_float),
@@ -114,6 +119,10 @@ _SIGS = {
                           C.c_int),
     "mpm_mark_neighboring_cells_grid_v": ([C.POINTER(MpmBuffers), C.POINTER(MpmReducedGrid), C.c_void_p], C.c_int),
     "mpm_g2p_sample": ([C.POINTER(MpmBuffers), C.POINTER(MpmReducedGrid), C.c_float, C.c_void_p], C.c_int),
+    "mpm_decoder_param_count": ([C.POINTER(MpmStressDecoder)], C.c_int64),
+    "mpm_decoder_forward": ([C.POINTER(MpmStressDecoder), C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
+    "mpm_decoder_stress": ([C.POINTER(MpmBuffers), C.POINTER(MpmStressDecoder), C.c_void_p, C.c_void_p, C.c_void_p],
+                           C.c_int),
     "mpm_svd3": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p], C.c_int),
     "mpm_return_map": ([C.POINTER(MpmScene), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                         C.c_int64, C.c_void_p], C.c_int),
@@ -175,10 +184,10 @@ def load(build_if_missing: bool = False) -> C.CDLL:
 
 
 def check_abi(lib: C.CDLL) -> None:
-    out = (C.c_int64 * 5)()
+    out = (C.c_int64 * 6)()
     lib.mpm_struct_sizes(out)
     mine = [C.sizeof(MpmCollider), C.sizeof(MpmScene), C.sizeof(MpmPlan), C.sizeof(MpmBuffers),
-            C.sizeof(MpmReducedGrid)]
+            C.sizeof(MpmReducedGrid), C.sizeof(MpmStressDecoder)]
     if list(out) != mine:
         raise ImportError(f"libmpm_gb300 ABI mismatch: library {list(out)} vs binding {mine}")
 

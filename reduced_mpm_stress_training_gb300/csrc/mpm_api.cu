@@ -155,6 +155,7 @@ void mpm_struct_sizes(int64_t *out) {
     out[2] = sizeof(MpmPlan);
     out[3] = sizeof(MpmBuffers);
     out[4] = sizeof(MpmReducedGrid);
+    out[5] = sizeof(MpmStressDecoder);
 }
 
 const char *mpm_error_string(int code) {
@@ -550,6 +551,32 @@ int mpm_g2p_sample(MpmBuffers *b, const MpmReducedGrid *g, float dt, void *strea
     if (r) return r;
     MPM_CHECK(mpm::launch_g2p_sample(make_ctx(b, stream, b->cur), *g, dt));
     b->keys_valid = 0;  // the sample points moved
+    return MPM_OK;
+}
+
+static bool decoder_ok(const MpmStressDecoder *d) {
+    return d && d->params && d->label_dim >= 0 && d->label_dim <= 64 && d->mu_dim >= 0 && d->mu_dim <= 4 &&
+           d->hidden >= 1 && d->hidden <= 64 && (d->siren == 0 || d->siren == 1) && d->omega_0 == d->omega_0;
+}
+
+int64_t mpm_decoder_param_count(const MpmStressDecoder *d) {
+    if (!d || d->label_dim < 0 || d->label_dim > 64 || d->mu_dim < 0 || d->mu_dim > 4 || d->hidden < 1 ||
+        d->hidden > 64)
+        return MPM_ERR_ARG;
+    return mpm::decoder_param_floats(*d);
+}
+
+int mpm_decoder_forward(const MpmStressDecoder *d, const float *rows, float *out, int64_t n, void *stream) {
+    if (!decoder_ok(d) || n < 0 || (n > 0 && (!rows || !out))) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_decoder_rows(*d, rows, out, n, num_sms(), static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
+int mpm_decoder_stress(MpmBuffers *b, const MpmStressDecoder *d, const float *label, const float *mu,
+                       void *stream) {
+    if (!buffers_ok(b) || !decoder_ok(d) || (d->label_dim > 0 && !label) || (d->mu_dim > 0 && !mu))
+        return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_decoder_stress(make_ctx(b, stream, b->cur), *d, label, mu));
     return MPM_OK;
 }
 

@@ -1,0 +1,285 @@
+// The reference's stress decoder NetDec
+// (offline_training_xhat_and_stress_and_mu/CROMnet_secondary.py:203-301, 434-525)
+// evaluated on the GPU: Prepare (standardise or clip the position), five
+// Linear layers of width `hidden` with ELU or sin(omega_0 x) activations,
+// the output Linear to the six stress components [xx, xy, xz, yy, yz, zz]
+// and invStandardizeQ.  Two forms:
+//   decoder_rows_kernel   -- NetDec.forward on caller rows (lbl + 3 + mu_dim
+//                            floats each) -> 6 floats per row
+//   decoder_stress_kernel -- the reduced-order loop's stress source: one
+//                            frame label for all particles, each particle's
+//                            x_initial from its state record and its mu row
+//                            by uid; the symmetric stress goes straight into
+//                            the record's stress words, which the next P2G
+//                            reads (the reference loads it with
+//                            load_uvstress_from_tensor, mpm_solver_warp.py:253-266).
+// FP32 throughout, as the reference's PyTorch module.  One thread per row;
+// the parameters (zero-padded to HP neurons) sit in shared memory and are
+// read as broadcasts, the activations stay in registers.
+#include "mpm_launch.h"
+
+namespace mpm {
+
+namespace {
+
+constexpr int kDecThreads = 128;
+
+struct DecLayout {  // float offsets of the shared-memory copy (HP-padded)
+    int w0, b0, wh, bh, we, be, prep, qm, qs, c0, total;
+};
+
+__host__ __device__ inline DecLayout dec_layout(int hp, int in) {
+    DecLayout L;
+    int o = 0;
+    L.w0 = o; o += hp * in;
+    L.b0 = o; o += hp;
+    L.wh = o; o += 4 * hp * hp;
+    L.bh = o; o += 4 * hp;
+    L.we = o; o += 6 * hp;
+    L.be = o; o += 8;
+    L.prep = o; o += 8;
+    L.qm = o; o += 8;
+    L.qs = o; o += 8;
+    L.c0 = o; o += hp;  // layer-0 bias plus the frame label's part (stress form)
+    L.total = o;
+    return L;
+}
+
+// offsets in the caller's packed (unpadded) parameter blob
+struct BlobLayout {
+    int w0, b0, wh, bh, we, be, prep, qm, qs, total;
+};
+
+__host__ __device__ inline BlobLayout blob_layout(int h, int in) {
+    BlobLayout B;
+    int o = 0;
+    B.w0 = o; o += h * in;
+    B.b0 = o; o += h;
+    B.wh = o; o += 4 * h * h;
+    B.bh = o; o += 4 * h;
+    B.we = o; o += 6 * h;
+    B.be = o; o += 6;
+    B.prep = o; o += 6;
+    B.qm = o; o += 6;
+    B.qs = o; o += 6;
+    B.total = o;
+    return B;
+}
+
+__device__ __forceinline__ float dec_act(float x, bool siren, float omega_0) {
+    if (siren) return sinf(__fmul_rn(omega_0, x));  // actSIN, :462-463
+    return x > 0.0f ? x : expm1f(x);                // actELU (F.elu, alpha 1), :459-460
+}
+
+// copy the blob into shared memory, padding every layer to hp neurons with zeros
+__device__ void dec_stage(const MpmStressDecoder &d, int hp, float *sm) {
+    const int h = d.hidden, in = d.label_dim + 3 + d.mu_dim;
+    const DecLayout L = dec_layout(hp, in);
+    const BlobLayout B = blob_layout(h, in);
+    const float *P = d.params;
+    for (int i = threadIdx.x; i < hp * in; i += blockDim.x) {
+        const int r = i / in, c = i % in;
+        sm[L.w0 + i] = r < h ? P[B.w0 + r * in + c] : 0.0f;
+    }
+    for (int i = threadIdx.x; i < hp; i += blockDim.x) sm[L.b0 + i] = i < h ? P[B.b0 + i] : 0.0f;
+    for (int i = threadIdx.x; i < 4 * hp * hp; i += blockDim.x) {
+        const int l = i / (hp * hp), r = (i / hp) % hp, c = i % hp;
+        sm[L.wh + i] = (r < h && c < h) ? P[B.wh + (l * h + r) * h + c] : 0.0f;
+    }
+    for (int i = threadIdx.x; i < 4 * hp; i += blockDim.x) {
+        const int l = i / hp, r = i % hp;
+        sm[L.bh + i] = r < h ? P[B.bh + l * h + r] : 0.0f;
+    }
+    for (int i = threadIdx.x; i < 6 * hp; i += blockDim.x) {
+        const int r = i / hp, c = i % hp;
+        sm[L.we + i] = c < h ? P[B.we + r * h + c] : 0.0f;
+    }
+    for (int i = threadIdx.x; i < 6; i += blockDim.x) {
+        sm[L.be + i] = P[B.be + i];
+        sm[L.prep + i] = P[B.prep + i];
+        sm[L.qm + i] = P[B.qm + i];
+        sm[L.qs + i] = P[B.qs + i];
+    }
+}
+
+// Prepare (:507-525): clipX 2 (x - min) / (max - min) - 1 for SIREN, else
+// standardizeX (x - mean) / std; prep holds (min, max) or (mean, std)
+__device__ __forceinline__ float dec_prep(const float *prep, int d, float x, bool siren) {
+    if (siren) return __fsub_rn(__fdiv_rn(__fmul_rn(2.0f, __fsub_rn(x, prep[d])), __fsub_rn(prep[3 + d], prep[d])), 1.0f);
+    return __fdiv_rn(__fsub_rn(x, prep[d]), prep[3 + d]);
+}
+
+// hidden layers dec1..dec4 and the output layer enc + invStandardizeQ (:476-477)
+template <int HP>
+__device__ __forceinline__ void dec_tail(const float *sm, const DecLayout &L, float h[HP], bool siren, float omega_0,
+                                         float q[6]) {
+#pragma unroll 1
+    for (int l = 0; l < 4; ++l) {
+        const float *W = sm + L.wh + l * HP * HP;
+        const float *b = sm + L.bh + l * HP;
+        float g[HP];
+#pragma unroll
+        for (int j = 0; j < HP; ++j) {
+            float acc = b[j];
+            const float4 *w4 = reinterpret_cast<const float4 *>(W + j * HP);
+#pragma unroll
+            for (int k = 0; k < HP / 4; ++k) {
+                const float4 w = w4[k];
+                acc = fmaf(w.x, h[4 * k + 0], acc);
+                acc = fmaf(w.y, h[4 * k + 1], acc);
+                acc = fmaf(w.z, h[4 * k + 2], acc);
+                acc = fmaf(w.w, h[4 * k + 3], acc);
+            }
+            g[j] = dec_act(acc, siren, omega_0);
+        }
+#pragma unroll
+        for (int j = 0; j < HP; ++j) h[j] = g[j];
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        float acc = sm[L.be + c];
+        const float4 *w4 = reinterpret_cast<const float4 *>(sm + L.we + c * HP);
+#pragma unroll
+        for (int k = 0; k < HP / 4; ++k) {
+            const float4 w = w4[k];
+            acc = fmaf(w.x, h[4 * k + 0], acc);
+            acc = fmaf(w.y, h[4 * k + 1], acc);
+            acc = fmaf(w.z, h[4 * k + 2], acc);
+            acc = fmaf(w.w, h[4 * k + 3], acc);
+        }
+        q[c] = __fadd_rn(sm[L.qm + c], __fmul_rn(acc, sm[L.qs + c]));
+    }
+}
+
+}  // namespace
+
+// NetDec.forward (:288-291) on rows (label_dim + 3 + mu_dim floats) -> 6 floats
+template <int HP>
+__global__ void __launch_bounds__(kDecThreads) decoder_rows_kernel(MpmStressDecoder d, const float *__restrict__ rows,
+                                                                   float *__restrict__ out, int64_t n) {
+    extern __shared__ float4 sm4[];
+    float *sm = reinterpret_cast<float *>(sm4);
+    const int L0 = d.label_dim, in = L0 + 3 + d.mu_dim;
+    const DecLayout L = dec_layout(HP, in);
+    dec_stage(d, HP, sm);
+    __syncthreads();
+    const bool siren = d.siren != 0;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const float *x = rows + r * in;
+        float h[HP];
+#pragma unroll
+        for (int j = 0; j < HP; ++j) h[j] = sm[L.b0 + j];
+        for (int k = 0; k < in; ++k) {
+            float v = x[k];
+            if (k >= L0 && k < L0 + 3) v = dec_prep(sm + L.prep, k - L0, v, siren);
+#pragma unroll
+            for (int j = 0; j < HP; ++j) h[j] = fmaf(sm[L.w0 + j * in + k], v, h[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < HP; ++j) h[j] = dec_act(h[j], siren, d.omega_0);
+        float q[6];
+        dec_tail<HP>(sm, L, h, siren, d.omega_0, q);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) out[r * 6 + c] = q[c];
+    }
+}
+
+// The decoder as the stress source of a substep: label (label_dim floats, the
+// frame's latent), each particle's x_initial from its record and mu row
+// (mu_dim floats, user order) by uid; writes the symmetric stress
+// [q0 q1 q2; q1 q3 q4; q2 q4 q5] into the record (mpm_solver_warp.py:383 order).
+template <int HP>
+__global__ void __launch_bounds__(kDecThreads) decoder_stress_kernel(MpmStressDecoder d, PState st,
+                                                                     const float *__restrict__ label,
+                                                                     const float *__restrict__ mu, int n) {
+    extern __shared__ float4 sm4[];
+    float *sm = reinterpret_cast<float *>(sm4);
+    const int L0 = d.label_dim, M = d.mu_dim, in = L0 + 3 + M;
+    const DecLayout L = dec_layout(HP, in);
+    dec_stage(d, HP, sm);
+    __syncthreads();
+    // the label's part of layer 0 is the same for every particle of the frame
+    for (int j = threadIdx.x; j < HP; j += blockDim.x) {
+        float acc = sm[L.b0 + j];
+        for (int k = 0; k < L0; ++k) acc = fmaf(sm[L.w0 + j * in + k], label[k], acc);
+        sm[L.c0 + j] = acc;
+    }
+    __syncthreads();
+    const bool siren = d.siren != 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 q0 = ldrec(st, i, 0), q1 = ldrec(st, i, 1);
+        const int uid = __float_as_int(q1.y);
+        float h[HP];
+#pragma unroll
+        for (int j = 0; j < HP; ++j) h[j] = sm[L.c0 + j];
+        const float xp[3] = {dec_prep(sm + L.prep, 0, q0.x, siren), dec_prep(sm + L.prep, 1, q0.y, siren),
+                             dec_prep(sm + L.prep, 2, q0.z, siren)};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int j = 0; j < HP; ++j) h[j] = fmaf(sm[L.w0 + j * in + L0 + k], xp[k], h[j]);
+        for (int k = 0; k < M; ++k) {
+            const float v = mu[(int64_t)uid * M + k];
+#pragma unroll
+            for (int j = 0; j < HP; ++j) h[j] = fmaf(sm[L.w0 + j * in + L0 + 3 + k], v, h[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < HP; ++j) h[j] = dec_act(h[j], siren, d.omega_0);
+        float q[6];
+        dec_tail<HP>(sm, L, h, siren, d.omega_0, q);
+        const float4 q5 = ldrec(st, i, 5);
+        strec(st, i, 5, make_float4(q5.x, q5.y, q5.z, q[0]));
+        strec(st, i, 6, make_float4(q[1], q[2], q[1], q[3]));
+        strec(st, i, 7, make_float4(q[4], q[2], q[4], q[5]));
+    }
+}
+
+int64_t decoder_param_floats(const MpmStressDecoder &d) {
+    return blob_layout(d.hidden, d.label_dim + 3 + d.mu_dim).total;
+}
+
+static int dec_hp(int hidden) { return hidden <= 32 ? 32 : 64; }
+
+static size_t dec_smem(const MpmStressDecoder &d) {
+    return (size_t)dec_layout(dec_hp(d.hidden), d.label_dim + 3 + d.mu_dim).total * sizeof(float);
+}
+
+template <typename K>
+static cudaError_t dec_prepare(K kernel, size_t smem) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t launch_decoder_rows(const MpmStressDecoder &d, const float *rows, float *out, int64_t n, int num_sms,
+                                cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const size_t smem = dec_smem(d);
+    const int64_t want = (n + kDecThreads - 1) / kDecThreads;
+    const int grid = (int)(want < (int64_t)num_sms * 8 ? want : (int64_t)num_sms * 8);
+    cudaError_t e;
+    if (dec_hp(d.hidden) == 32) {
+        if ((e = dec_prepare(decoder_rows_kernel<32>, smem)) != cudaSuccess) return e;
+        decoder_rows_kernel<32><<<grid, kDecThreads, smem, stream>>>(d, rows, out, n);
+    } else {
+        if ((e = dec_prepare(decoder_rows_kernel<64>, smem)) != cudaSuccess) return e;
+        decoder_rows_kernel<64><<<grid, kDecThreads, smem, stream>>>(d, rows, out, n);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_decoder_stress(const Ctx &cx, const MpmStressDecoder &d, const float *label, const float *mu) {
+    if (cx.n == 0) return cudaSuccess;
+    const size_t smem = dec_smem(d);
+    const int want = (cx.n + kDecThreads - 1) / kDecThreads;
+    const int grid = want < cx.num_sms * 8 ? want : cx.num_sms * 8;
+    cudaError_t e;
+    if (dec_hp(d.hidden) == 32) {
+        if ((e = dec_prepare(decoder_stress_kernel<32>, smem)) != cudaSuccess) return e;
+        decoder_stress_kernel<32><<<grid, kDecThreads, smem, cx.stream>>>(d, cx.st, label, mu, cx.n);
+    } else {
+        if ((e = dec_prepare(decoder_stress_kernel<64>, smem)) != cudaSuccess) return e;
+        decoder_stress_kernel<64><<<grid, kDecThreads, smem, cx.stream>>>(d, cx.st, label, mu, cx.n);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace mpm

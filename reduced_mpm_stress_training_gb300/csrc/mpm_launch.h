@@ -71,6 +71,12 @@ cudaError_t launch_svd3(const float *A, float *U, float *s, float *V, int64_t n,
 cudaError_t launch_return_map(const MpmScene &scene, const float *Ft, float *yld, float *F,
                               float *tau, int64_t n, cudaStream_t st);
 
+// the reference's stress decoder (mpm_decoder.cu); see mpm_decoder_forward / mpm_decoder_stress
+int64_t decoder_param_floats(const MpmStressDecoder &d);
+cudaError_t launch_decoder_rows(const MpmStressDecoder &d, const float *rows, float *out, int64_t n, int num_sms,
+                                cudaStream_t stream);
+cudaError_t launch_decoder_stress(const Ctx &cx, const MpmStressDecoder &d, const float *label, const float *mu);
+
 // slot_of_uid[uid] = slot of the live state (mpm_io.cu)
 cudaError_t launch_slot_of_uid(const Ctx &cx);
 

@@ -236,6 +236,19 @@ class MPMSimulator:
                                    torch.as_tensor(tensor_stress))
 
     # extensions (no reference counterpart)
+    def load_stress_from_decoder(self, decoder, label, mu=None):
+        """The reduced-order loop's stress source: decode every particle's stress
+        with a ``decoder.StressDecoder`` (NetDec, CROMnet_secondary.py:203-301) from
+        the frame's label, the particle's x_initial and its mu row, straight into
+        the state the next p2g2p reads (the reference decodes on the host side and
+        calls load_uvstress_from_tensor, :253-266).  mu defaults to the friction
+        angle of every particle, the parameter the reference's frames carry
+        (:385-386)."""
+        if mu is None and decoder.mu_dim == 1:
+            mu = torch.full((self.n_particles, 1), float(self._params.friction_angle),
+                            dtype=torch.float32, device=self.device)
+        decoder.stress_into(self._engine, label, mu)
+
     def load_vol_from_tensor(self, tensor_vol):
         self._engine.load(A.FIELD_VOL, tensor_vol)
 

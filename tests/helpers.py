@@ -92,3 +92,29 @@ def within_fp32_floor(gpu, o32, o64, rtol=1e-5, k=3.0):
     lim = max(rtol * scale, k * floor)
     ok = (d64 <= lim) or ((d32 <= lim) and (d64 <= lim + floor))
     return bool(ok), dict(gpu_vs_o32=d32 / scale, gpu_vs_o64=d64 / scale, o32_vs_o64=floor / scale)
+
+
+def netdec_torch(sd: dict, rows, label_dim: int, siren: bool, omega_0: float):
+    """PyTorch float32 restatement of NetDec.forward
+    (offline_training_xhat_and_stress_and_mu/CROMnet_secondary.py:203-301, 447-525):
+    the float32 reference the decoder kernels are compared with."""
+    import torch.nn.functional as Fn
+
+    sd = {k[len("decoder."):] if k.startswith("decoder.") else k: torch.as_tensor(v, dtype=torch.float32)
+          for k, v in sd.items()}
+    x = torch.as_tensor(rows, dtype=torch.float32).clone()
+    xs = x[:, label_dim:label_dim + 3]
+    if siren:
+        lo, hi = sd["prepare.min_x_torch"], sd["prepare.max_x_torch"]
+        x[:, label_dim:label_dim + 3] = 2 * (xs - lo) / (hi - lo) - 1
+    else:
+        x[:, label_dim:label_dim + 3] = (xs - sd["prepare.mean_x_torch"]) / sd["prepare.std_x_torch"]
+
+    def act(z):
+        return torch.sin(omega_0 * z) if siren else Fn.elu(z)
+
+    h = x
+    for name in ("dec0", "dec1", "dec2", "dec3", "dec4"):
+        h = act(Fn.linear(h, sd[f"{name}.weight"], sd[f"{name}.bias"]))
+    q = Fn.linear(h, sd["enc.weight"], sd["enc.bias"])
+    return sd["invStandardizeQ.mean_q_torch"] + q * sd["invStandardizeQ.std_q_torch"]

@@ -38,11 +38,11 @@ def test_library_loads_and_exports_every_declared_symbol(built):
 
 def test_struct_sizes_match_binding(built):
     lib = A.load()
-    out = (C.c_int64 * 5)()
+    out = (C.c_int64 * 6)()
     lib.mpm_struct_sizes(out)
     assert list(out) == [C.sizeof(A.MpmCollider), C.sizeof(A.MpmScene), C.sizeof(A.MpmPlan),
-                         C.sizeof(A.MpmBuffers), C.sizeof(A.MpmReducedGrid)]
-    assert C.sizeof(A.MpmReducedGrid) == 88
+                         C.sizeof(A.MpmBuffers), C.sizeof(A.MpmReducedGrid), C.sizeof(A.MpmStressDecoder)]
+    assert C.sizeof(A.MpmReducedGrid) == 88 and C.sizeof(A.MpmStressDecoder) == 32
     assert lib.mpm_abi_version() == 3
 
 
