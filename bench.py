@@ -17,6 +17,8 @@ One JSON line on rank 0.  A "step" is one substep of every particle.
             memory (export_uvFstress_from_warp)
   --workload reduced_1m -- the reduced sampled-quadrature substep
             (p2g2p_reduced) on the same column with 4,096 sample points
+  --workload decoder_1m -- the substep with the reference's stress decoder
+            (NetDec) decoding every particle's stress first
   --impl reference -- the CPU restatement of the reference's algorithm (the
             reference is Python + Warp and cannot be installed here) on all
             host cores, on a bounded particle sample per step.
@@ -646,6 +648,70 @@ def reduced_arm(args):
         "status": sim.engine.status()}), flush=True)
 
 
+def decoder_arm(args):
+    """The reduced-order loop's substep with the reference's stress decoder as the
+    stress source (NetDec 10 -> 30 x 5 -> 6, ELU, seeded reference initialisation):
+    each step decodes every particle's stress into the state (mpm_decoder_stress)
+    and runs the substep, on the large sand column.  CUDA events."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as g
+    from reduced_mpm_stress_training_gb300 import MPM_Simulator_WARP
+    from reduced_mpm_stress_training_gb300 import scenarios as S
+    from reduced_mpm_stress_training_gb300.decoder import StressDecoder
+
+    g.build()
+    sc = S.sand_column_1m()
+    n, dt = sc.n_particles, sc.dt
+    device = torch.device("cuda:0")
+    x0, v0, vol, mass = sc.particles()
+    sim = MPM_Simulator_WARP(n, n_grid=sc.n_grid, grid_lim=sc.grid_lim, device=device)
+    sim.set_parameters(material=sc.material, E=sc.E, nu=sc.nu, friction_angle=sc.friction_angle,
+                       gravity=sc.gravity)
+    sim.load_x_initial_from_tensor(torch.from_numpy(x0))
+    sim.load_vol_from_tensor(torch.from_numpy(vol))
+    sim.load_mass_from_tensor(torch.from_numpy(mass))
+    sim.load_v_from_tensor(torch.from_numpy(v0))
+    for kind, kw in sc.colliders():
+        sim.add_surface_collider(**kw) if kind == "surface" else sim.add_bounding_box(**kw)
+    dec = StressDecoder.random(seed=0, x_stats=((0.5, 0.5, 0.45), (0.09, 0.09, 0.23)),
+                               q_stats=((0.0,) * 6, (50.0,) * 6), device=device)
+    label = torch.from_numpy(np.random.default_rng(0).normal(0, 1, 6).astype(np.float32)).to(device)
+    mu = torch.full((n, 1), sc.friction_angle, dtype=torch.float32, device=device)
+    eng = sim.engine
+
+    def decode():
+        dec.stress_into(eng, label, mu)
+
+    def step():
+        decode()
+        eng.substep_raw(float(sim.time), dt)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+        sim.time += dt
+    sim.check_status()
+    K = max(16, min(args.steps, 1000))
+    t_dec = _events_ms(decode, K) / 1e3
+    t_step = _events_ms(step, K) / 1e3
+    sim.time += K * dt
+    flops = 2 * (3 * dec.hidden + dec.mu_dim * dec.hidden + 4 * dec.hidden ** 2 + 6 * dec.hidden) * n
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    fp32_peak = sms * 128 * 2 * 2.07e9 / 1e12
+    print(json.dumps({
+        "metric": "particle-substeps/s (decoded-stress substep: NetDec stress + p2g2p, 1M sand, fp32)",
+        "value": n / t_step, "unit": "particle-substeps/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded reference initialisation of the decoder)",
+        "config": {"workload": f"sand_column_1m: {n} particles, {sc.n_grid}^3 grid; NetDec label 6, "
+                               f"hidden {dec.hidden}, ELU",
+                   "l2": "state larger than L2"},
+        "decoder": {"ms": 1e3 * t_dec, "tflops": flops / t_dec / 1e12, "flops_per_particle": flops / n,
+                    "fp32_peak_nominal_tflops": fp32_peak, "frac_of_nominal": flops / t_dec / 1e12 / fp32_peak},
+        "status": eng.status()}), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
@@ -654,6 +720,10 @@ def main():
     if args.workload == "batch_64":
         if rank == 0 and args.impl == "gb300":
             batched_arm(args)
+        return
+    if args.workload == "decoder_1m":
+        if rank == 0 and args.impl == "gb300":
+            decoder_arm(args)
         return
     if args.workload == "reduced_1m":
         if rank == 0 and args.impl == "gb300":

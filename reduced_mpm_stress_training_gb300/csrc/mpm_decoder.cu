@@ -66,9 +66,28 @@ __host__ __device__ inline BlobLayout blob_layout(int h, int in) {
     return B;
 }
 
+// exp(x) - 1 for x <= 0: on [-0.5, 0] the Taylor series through x^8 / 8!
+// (truncation below 1.1e-8 of the result), below that exp(x) - 1, whose
+// magnitude is then at least 0.39, so the 2^-21 relative error of the fast
+// exponential stays under 1e-6 of it
+__device__ __forceinline__ float expm1_nonpos(float x) {
+    if (x > -0.5f) {
+        float p = 1.0f / 40320.0f;
+        p = fmaf(p, x, 1.0f / 5040.0f);
+        p = fmaf(p, x, 1.0f / 720.0f);
+        p = fmaf(p, x, 1.0f / 120.0f);
+        p = fmaf(p, x, 1.0f / 24.0f);
+        p = fmaf(p, x, 1.0f / 6.0f);
+        p = fmaf(p, x, 0.5f);
+        p = fmaf(p, x, 1.0f);
+        return p * x;
+    }
+    return __expf(x) - 1.0f;
+}
+
 __device__ __forceinline__ float dec_act(float x, bool siren, float omega_0) {
     if (siren) return sinf(__fmul_rn(omega_0, x));  // actSIN, :462-463
-    return x > 0.0f ? x : expm1f(x);                // actELU (F.elu, alpha 1), :459-460
+    return x > 0.0f ? x : expm1_nonpos(x);          // actELU (F.elu, alpha 1), :459-460
 }
 
 // copy the blob into shared memory, padding every layer to hp neurons with zeros
@@ -244,9 +263,21 @@ static size_t dec_smem(const MpmStressDecoder &d) {
     return (size_t)dec_layout(dec_hp(d.hidden), d.label_dim + 3 + d.mu_dim).total * sizeof(float);
 }
 
+// opt each kernel in to the largest shared-memory copy once per device (not a
+// stream operation, so launches stay capturable in CUDA graphs afterwards)
 template <typename K>
-static cudaError_t dec_prepare(K kernel, size_t smem) {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+static cudaError_t dec_prepare(K kernel, int slot) {
+    static bool done[4][64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (done[slot][dev]) return cudaSuccess;
+    const int in_max = 64 + 3 + 4;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(dec_layout(64, in_max).total * sizeof(float)));
+    if (e == cudaSuccess) done[slot][dev] = true;
+    return e;
 }
 
 cudaError_t launch_decoder_rows(const MpmStressDecoder &d, const float *rows, float *out, int64_t n, int num_sms,
@@ -257,10 +288,10 @@ cudaError_t launch_decoder_rows(const MpmStressDecoder &d, const float *rows, fl
     const int grid = (int)(want < (int64_t)num_sms * 8 ? want : (int64_t)num_sms * 8);
     cudaError_t e;
     if (dec_hp(d.hidden) == 32) {
-        if ((e = dec_prepare(decoder_rows_kernel<32>, smem)) != cudaSuccess) return e;
+        if ((e = dec_prepare(decoder_rows_kernel<32>, 0)) != cudaSuccess) return e;
         decoder_rows_kernel<32><<<grid, kDecThreads, smem, stream>>>(d, rows, out, n);
     } else {
-        if ((e = dec_prepare(decoder_rows_kernel<64>, smem)) != cudaSuccess) return e;
+        if ((e = dec_prepare(decoder_rows_kernel<64>, 1)) != cudaSuccess) return e;
         decoder_rows_kernel<64><<<grid, kDecThreads, smem, stream>>>(d, rows, out, n);
     }
     return cudaGetLastError();
@@ -273,10 +304,10 @@ cudaError_t launch_decoder_stress(const Ctx &cx, const MpmStressDecoder &d, cons
     const int grid = want < cx.num_sms * 8 ? want : cx.num_sms * 8;
     cudaError_t e;
     if (dec_hp(d.hidden) == 32) {
-        if ((e = dec_prepare(decoder_stress_kernel<32>, smem)) != cudaSuccess) return e;
+        if ((e = dec_prepare(decoder_stress_kernel<32>, 2)) != cudaSuccess) return e;
         decoder_stress_kernel<32><<<grid, kDecThreads, smem, cx.stream>>>(d, cx.st, label, mu, cx.n);
     } else {
-        if ((e = dec_prepare(decoder_stress_kernel<64>, smem)) != cudaSuccess) return e;
+        if ((e = dec_prepare(decoder_stress_kernel<64>, 3)) != cudaSuccess) return e;
         decoder_stress_kernel<64><<<grid, kDecThreads, smem, cx.stream>>>(d, cx.st, label, mu, cx.n);
     }
     return cudaGetLastError();
