@@ -211,6 +211,15 @@ int mpm_export_uvFstress(MpmBuffers *b, float *u, float *v, float *F_disp, float
  * left in flight on the current device. */
 int mpm_sync_transfers(void);
 
+/* The arrays of one frame file (save_data_at_frame, mpm_solver_warp.py:339-404)
+ * in its transposed layout, one pass: out (34 * n floats, device) holds
+ * x (3, n) = x_initial, q (3, n) = u, masses (1, n), f_tensor (9, n) = F - I
+ * row-major, stress (6, n) = components 0, 1, 2, 4, 5, 8 of the row-major
+ * stress, v (3, n), C (9, n) -- row c of each array is component c of every
+ * particle in user order. */
+#define MPM_FRAME_FLOATS_PER_PARTICLE 34
+int mpm_export_frame(MpmBuffers *b, float *out, void *stream);
+
 /* ---- the substep ----------------------------------------------------- */
 
 /* One full substep for every scene: x = x0 + u, cell-block sort, APIC P2G

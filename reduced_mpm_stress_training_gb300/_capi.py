@@ -108,6 +108,7 @@ _SIGS = {
     "mpm_export_uvFstress": ([C.POINTER(MpmBuffers), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                               C.c_void_p], C.c_int),
     "mpm_sync_transfers": ([], C.c_int),
+    "mpm_export_frame": ([C.POINTER(MpmBuffers), C.c_void_p, C.c_void_p], C.c_int),
     "mpm_p2g2p": ([C.POINTER(MpmBuffers), C.c_float, C.c_float, C.c_void_p], C.c_int),
     "mpm_sort": ([C.POINTER(MpmBuffers), C.c_void_p], C.c_int),
     "mpm_p2g": ([C.POINTER(MpmBuffers), C.c_float, C.c_void_p], C.c_int),

@@ -370,6 +370,12 @@ int mpm_export_uvFstress(MpmBuffers *b, float *u, float *v, float *F_disp, float
     return MPM_OK;
 }
 
+int mpm_export_frame(MpmBuffers *b, float *out, void *stream) {
+    if (!buffers_ok(b) || (b->plan.n_particles > 0 && !out)) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_export_frame(make_ctx(b, stream, b->cur), out));
+    return MPM_OK;
+}
+
 int mpm_sort(MpmBuffers *b, void *stream) {
     if (!buffers_ok(b)) return MPM_ERR_ARG;
     mpm::Ctx cx = make_ctx(b, stream, b->cur);

@@ -120,6 +120,33 @@ __global__ void export_uvFstress_kernel(PState st, int n, const int *__restrict_
     pt[5] = q7.x; pt[6] = q7.y; pt[7] = q7.z; pt[8] = q7.w;
 }
 
+// save_data_at_frame's arrays (mpm_solver_warp.py:339-404) in one pass, in the
+// frame file's own transposed layout: row c of an array holds component c of
+// every particle in user order, so each store instruction of a warp writes 32
+// consecutive floats.  out: x_initial (3, n) | q = u (3, n) | masses (1, n) |
+// f_tensor = F - I (9, n) | stress components 0,1,2,4,5,8 (6, n) | v (3, n) |
+// C (9, n).
+__global__ void export_frame_kernel(PState st, int n, const int *__restrict__ inv, float *__restrict__ out) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const int i = inv[id];
+    const float4 q0 = ldrec(st, i, 0), q1 = ldrec(st, i, 1), q2 = ldrec(st, i, 2), q3 = ldrec(st, i, 3),
+                 q4 = ldrec(st, i, 4), q5 = ldrec(st, i, 5), q6 = ldrec(st, i, 6), q7 = ldrec(st, i, 7),
+                 q8 = ldrec(st, i, 8), q9 = ldrec(st, i, 9);
+    const int64_t N = n;
+    float *o = out + id;
+    const float rows[34] = {
+        q0.x, q0.y, q0.z,                                                                    // x
+        q2.x, q2.y, q2.z,                                                                    // q
+        q0.w,                                                                                // masses
+        q8.x - 1.0f, q8.y, q8.z, q8.w, q9.x - 1.0f, q9.y, q9.z, q9.w, q1.w - 1.0f,           // f_tensor
+        q5.w, q6.x, q6.y, q6.w, q7.x, q7.w,                                                  // stress
+        q2.w, q3.x, q3.y,                                                                    // v
+        q3.z, q3.w, q4.x, q4.y, q4.z, q4.w, q5.x, q5.y, q5.z};                               // C
+#pragma unroll
+    for (int r = 0; r < 34; ++r) o[r * N] = rows[r];
+}
+
 // dense (n,n,n) grid_m / grid_v_in from the accumulator (valid after p2g)
 __global__ void export_acc_kernel(const float4 *__restrict__ acc, int64_t block_begin, int nb, int n,
                                   float *gm, float *gvin) {
@@ -215,6 +242,13 @@ cudaError_t launch_export_uvFstress(const Ctx &cx, float *u, float *v, float *fd
     slot_of_uid_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, cx.ws.slot_of_uid);
     export_uvFstress_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, cx.ws.slot_of_uid, u, v,
                                                                            fd, tau);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_frame(const Ctx &cx, float *out) {
+    if (cx.n == 0) return cudaSuccess;
+    slot_of_uid_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, cx.ws.slot_of_uid);
+    export_frame_kernel<<<blocks_for(cx.n, 256), 256, 0, cx.stream>>>(cx.st, cx.n, cx.ws.slot_of_uid, out);
     return cudaGetLastError();
 }
 

@@ -65,6 +65,7 @@ cudaError_t launch_export(const Ctx &cx, int field, float *dst);
 cudaError_t launch_advance_colliders(MpmScene *scenes, int n_scenes, float time, float dt, cudaStream_t stream);
 cudaError_t launch_load_uvstress(const Ctx &cx, const float *u, const float *v, const float *tau);
 cudaError_t launch_export_uvFstress(const Ctx &cx, float *u, float *v, float *fd, float *tau);
+cudaError_t launch_export_frame(const Ctx &cx, float *out);
 cudaError_t launch_export_grid(const Ctx &cx, const MpmScene &host_scene, int scene_index,
                                float *gm, float *gvin, float *gvout);
 cudaError_t launch_svd3(const float *A, float *U, float *s, float *V, int64_t n, cudaStream_t st);

@@ -36,9 +36,14 @@ the current PyTorch CUDA stream.  Differences a caller can see:
 """
 from __future__ import annotations
 
+import ctypes
+import os
+
+import numpy as np
 import torch
 
 from . import _capi as A
+from . import frames as FR
 from .engine import (Collider, MPMEngine, MPMStatusError, ReducedGrid, SceneParams, lame_from_E_nu,
                      material_code, dp_alpha)
 
@@ -134,6 +139,8 @@ class MPMSimulator:
         self._sample_index = torch.zeros(1, dtype=torch.int32, device=self.device)
         self._reduced = None
         self._grid_from_reduced = False
+        # colour for the OBJ output (mpm_solver_warp.py:71)
+        self.particle_color = np.ones(self.n_particles, dtype=float)
         self.time = 0.0
         self.mpm_model = _Model(self)
         self.mpm_state = _State(self)
@@ -293,6 +300,93 @@ class MPMSimulator:
         u, v, fd, st = self._engine.export_uvFstress()
         fd = self._f_disp_loaded.clone() if self._f_disp_loaded is not None else fd.reshape(n, 3, 3)
         return u.reshape(n, 3), v.reshape(n, 3), fd, st.reshape(n, 3, 3)
+
+    # --------------------------------------------------------------- frame files
+    def export_frame_arrays(self) -> dict:
+        """The float32 arrays of one frame file in its transposed layout
+        (mpm_export_frame, one device pass), as NumPy arrays."""
+        n = self.n_particles
+        buf = torch.empty(34 * n, dtype=torch.float32, device=self.device)
+        eng = self._engine
+        A.check(eng.lib.mpm_export_frame(ctypes.byref(eng.buf), buf.data_ptr(), eng.stream), "mpm_export_frame")
+        arrays = FR.split_frame_buffer(buf.cpu().numpy(), n)
+        if self._f_disp_loaded is not None:  # F_disp held apart from F (load_uvF, reduced substep)
+            arrays["f_tensor"] = self._f_disp_loaded.reshape(n, 9).t().contiguous().cpu().numpy()
+        return arrays
+
+    def save_data_at_frame(self, dir_name, frame, include_parameter="friction_angle", save_to_h5=True,
+                           save_to_obj=True, save_visual_F=False):
+        """engine_stress/mpm_solver_warp.py:339-404: x, q, time, masses, f_tensor,
+        stress (6 components), v, mu, C to dir_name/h5_f_<frame>.h5 (.npz without
+        h5py), positions to the matching .obj.  The process umask is left alone
+        (the reference sets it to 0) and the debug prints are dropped."""
+        os.makedirs(dir_name, 0o777, exist_ok=True)
+        fullfilename = FR.frame_filename(dir_name, frame)
+        stem = fullfilename[: fullfilename.rindex(".")]
+        if save_to_obj:
+            self.particle_position2obj(stem + ".obj")
+        if save_visual_F:
+            self.particle_F_norm2obj(dir_name + "/visualF_f_" + str(frame).zfill(10) + ".obj")
+        if include_parameter and include_parameter != "friction_angle":
+            raise ValueError(f"include_parameter {include_parameter!r}: only 'friction_angle' is defined")
+        if not save_to_h5:
+            return
+        a = self.export_frame_arrays()
+        n = self.n_particles
+        data = {"x": a["x"], "q": a["q"], "time": np.array([self.time]).reshape(1, 1), "masses": a["masses"],
+                "f_tensor": a["f_tensor"], "stress": a["stress"], "v": a["v"]}
+        if include_parameter:
+            data["mu"] = np.ones((1, n)) * self._params.friction_angle
+        data["C"] = a["C"]
+        FR.write_frame(fullfilename, data)
+
+    def particle_position2obj(self, fullfilename):
+        """engine_stress/mpm_solver_warp.py:312-322: 'v x y z c c c' per particle,
+        current positions, c = 1 - 1 / particle_color (all ones: 0.0)."""
+        x = self._engine.export(A.FIELD_X).reshape(self.n_particles, 3).cpu().numpy()
+        col = 1.0 - 1.0 / self.particle_color
+        with open(fullfilename, "w") as f:
+            f.write(FR.obj_lines(x, [(c, c, c) for c in col]))
+
+    def particle_F_norm2obj(self, fullfilename, F_upperbound=2.0):
+        """engine_stress/mpm_solver_warp.py:324-336: initial positions coloured by
+        min(1, |F_disp| / F_upperbound)."""
+        n = self.n_particles
+        x0 = self._engine.export(A.FIELD_X_INITIAL).reshape(n, 3).cpu().numpy()
+        fd = self._f_disp().reshape(n, 9).cpu().numpy()
+        norm = np.linalg.norm(fd, axis=1)
+        with open(fullfilename, "w") as f:
+            f.write(FR.obj_lines(x0, [(np.minimum(1.0, c / F_upperbound), 0, 0) for c in norm]))
+
+    def load_from_sampling(self, sampling_h5, n_grid=100, grid_lim=1.0, device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:129-153: re-initialise for the file's
+        particles; x_initial = x, v = 0, F_disp = f_tensor, F = I, mass, density,
+        volume.  A missing file raises FileNotFoundError (the reference exits)."""
+        d = FR.read_frame(FR.resolve(sampling_h5))
+        x = np.asarray(d["x"]).transpose()
+        q = np.asarray(d["q"]).transpose()
+        n = q.shape[0]
+        self.initialize(n, n_grid, grid_lim, device=device)
+        mass = np.squeeze(np.asarray(d["masses"]), 0)
+        density = np.squeeze(np.asarray(d["particle_density"]), 0)
+        vol = np.squeeze(np.asarray(d["particle_volume"]), 0)
+        self.load_x_initial_from_tensor(torch.from_numpy(np.ascontiguousarray(x, np.float32)))
+        self.load_mass_from_tensor(torch.from_numpy(np.ascontiguousarray(mass, np.float32)))
+        self.load_vol_from_tensor(torch.from_numpy(np.ascontiguousarray(vol, np.float32)))
+        self._density = torch.from_numpy(np.ascontiguousarray(density, np.float32)).to(self.device)
+        f = np.ascontiguousarray(np.asarray(d["f_tensor"], np.float32).reshape(n, 3, 3))
+        self._f_disp_loaded = torch.from_numpy(f).to(self.device)
+
+    def load_uvFstress_from_h5(self, h5filename, sample_point=0, device="cuda:0"):
+        """engine_stress/mpm_solver_warp.py:268-303: u = q, v, stress from its six
+        components; f_tensor is read but, as there, not loaded."""
+        d = FR.read_frame(FR.resolve(h5filename))
+        q = np.asarray(d["q"]).transpose()
+        v = np.asarray(d["v"]).transpose()
+        stress = FR.stress_from_components(np.asarray(d["stress"]).transpose())
+        self.load_uvstress_from_tensor(torch.from_numpy(np.ascontiguousarray(q, np.float32)),
+                                       torch.from_numpy(np.ascontiguousarray(v, np.float32)),
+                                       torch.from_numpy(np.ascontiguousarray(stress, np.float32)))
 
     # --------------------------------------------------------------- colliders
     def add_surface_collider(self, point, normal, surface="sticky", friction=0.0,
