@@ -1,5 +1,6 @@
 // C ABI of libmpm_gb300.so (declared in include/mpm_gb300.h): buffer layout,
 // argument checks, and the launch sequence of the substep.
+#include <nvtx3/nvToolsExt.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -13,6 +14,15 @@ int fail_cuda(cudaError_t e) {
     snprintf(g_cuda_err, sizeof(g_cuda_err), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
     return MPM_ERR_CUDA;
 }
+
+// NVTX range over one entry point, so a profiler's timeline shows the library's
+// stages by name (header-only NVTX 3: a no-op unless a tool is attached)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 #define MPM_CHECK(expr)                          \
     do {                                         \
@@ -318,6 +328,7 @@ int mpm_sync_transfers(void) {
 
 int mpm_load_uvstress(MpmBuffers *b, const float *u, const float *v, const float *stress, int32_t src_on_host,
                       void *stream) {
+    NvtxRange nvtx_("mpm_load_uvstress");
     if (!buffers_ok(b) || (b->plan.n_particles > 0 && (!u || !v || !stress))) return MPM_ERR_ARG;
     mpm::Ctx cx = make_ctx(b, stream, b->cur);
     if (cx.n == 0) return MPM_OK;
@@ -344,6 +355,7 @@ int mpm_load_uvstress(MpmBuffers *b, const float *u, const float *v, const float
 
 int mpm_export_uvFstress(MpmBuffers *b, float *u, float *v, float *F_disp, float *stress, int32_t dst_on_host,
                          void *stream) {
+    NvtxRange nvtx_("mpm_export_uvFstress");
     if (!buffers_ok(b) || (b->plan.n_particles > 0 && (!u || !v || !F_disp || !stress))) return MPM_ERR_ARG;
     mpm::Ctx cx = make_ctx(b, stream, b->cur);
     if (cx.n == 0) return MPM_OK;
@@ -371,12 +383,14 @@ int mpm_export_uvFstress(MpmBuffers *b, float *u, float *v, float *F_disp, float
 }
 
 int mpm_export_frame(MpmBuffers *b, float *out, void *stream) {
+    NvtxRange nvtx_("mpm_export_frame");
     if (!buffers_ok(b) || (b->plan.n_particles > 0 && !out)) return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_export_frame(make_ctx(b, stream, b->cur), out));
     return MPM_OK;
 }
 
 int mpm_sort(MpmBuffers *b, void *stream) {
+    NvtxRange nvtx_("mpm_sort");
     if (!buffers_ok(b)) return MPM_ERR_ARG;
     mpm::Ctx cx = make_ctx(b, stream, b->cur);
     if (!b->keys_valid) {
@@ -390,12 +404,14 @@ int mpm_sort(MpmBuffers *b, void *stream) {
 }
 
 int mpm_p2g(MpmBuffers *b, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_p2g");
     if (!buffers_ok(b)) return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_p2g(make_ctx(b, stream, b->cur), dt));
     return MPM_OK;
 }
 
 int mpm_grid_update(MpmBuffers *b, float time, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_grid_update");
     if (!buffers_ok(b)) return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_grid(make_ctx(b, stream, b->cur), time, dt));
     if (b->collider_flags & MPM_CF_MOVING)  // after every node used the old points
@@ -405,6 +421,7 @@ int mpm_grid_update(MpmBuffers *b, float time, float dt, void *stream) {
 }
 
 int mpm_g2p(MpmBuffers *b, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_g2p");
     if (!buffers_ok(b)) return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_g2p(make_ctx(b, stream, b->cur), dt));
     b->cur ^= 1;  // G2P wrote the sorted, updated records into the other buffer
@@ -413,6 +430,7 @@ int mpm_g2p(MpmBuffers *b, float dt, void *stream) {
 }
 
 int mpm_p2g2p(MpmBuffers *b, float time, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_p2g2p");
     int r = mpm_sort(b, stream);
     if (r) return r;
     if ((r = mpm_p2g(b, dt, stream))) return r;
@@ -460,6 +478,7 @@ int mpm_surrogate_apply(const MpmScene *scene, const void *mlp_params, const Mpm
 
 int mpm_g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogateConfig *cfg, void *fallback,
                       int32_t *stats, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_g2p_surrogate");
     if (!buffers_ok(b) || !mlp_params || !surrogate_cfg_ok(cfg) || !stats) return MPM_ERR_ARG;
     if (b->plan.n_particles > 0 && (!fallback || (reinterpret_cast<uintptr_t>(fallback) & 7))) return MPM_ERR_ARG;
     if (reinterpret_cast<uintptr_t>(mlp_params) & 15) return MPM_ERR_ARG;
@@ -473,6 +492,7 @@ int mpm_g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogateC
 
 int mpm_p2g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogateConfig *cfg, void *fallback,
                         int32_t *stats, float time, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_p2g2p_surrogate");
     if (!buffers_ok(b) || !mlp_params || !surrogate_cfg_ok(cfg) || !stats) return MPM_ERR_ARG;
     int r = mpm_sort(b, stream);
     if (r) return r;
@@ -483,6 +503,7 @@ int mpm_p2g2p_surrogate(MpmBuffers *b, const void *mlp_params, const MpmSurrogat
 
 int mpm_adjoint_substep(MpmBuffers *b, const float *adj_out, float *adj_in, void *grid_adj, double *theta_bar,
                         float time, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_adjoint_substep");
     if (!buffers_ok(b) || !theta_bar || !grid_adj) return MPM_ERR_ARG;
     if (b->plan.n_particles > 0 && (!adj_out || !adj_in || adj_out == adj_in)) return MPM_ERR_ARG;
     if (reinterpret_cast<uintptr_t>(grid_adj) & 15) return MPM_ERR_ARG;
@@ -498,12 +519,14 @@ int64_t mpm_substep_grid_bytes(const MpmPlan *plan) {
 }
 
 int mpm_save_substep_grid(MpmBuffers *b, void *dst, void *stream) {
+    NvtxRange nvtx_("mpm_save_substep_grid");
     if (!buffers_ok(b) || !dst || (reinterpret_cast<uintptr_t>(dst) & 255)) return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_save_grid(make_ctx(b, stream, b->cur), dst));
     return MPM_OK;
 }
 
 int mpm_load_substep_grid(MpmBuffers *b, const void *src, void *stream) {
+    NvtxRange nvtx_("mpm_load_substep_grid");
     if (!buffers_ok(b) || !src || (reinterpret_cast<uintptr_t>(src) & 255)) return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_load_grid(make_ctx(b, stream, b->cur), src));
     return MPM_OK;
@@ -536,6 +559,7 @@ static int reduced_args_ok(const MpmBuffers *b, const MpmReducedGrid *g) {
 }
 
 int mpm_p2g2p_reduced(MpmBuffers *b, const MpmReducedGrid *g, float time, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_p2g2p_reduced");
     int r = reduced_args_ok(b, g);
     if (r) return r;
     MPM_CHECK(mpm::launch_p2g2p_reduced(make_ctx(b, stream, b->cur), *g, time, dt));
@@ -546,6 +570,7 @@ int mpm_p2g2p_reduced(MpmBuffers *b, const MpmReducedGrid *g, float time, float 
 }
 
 int mpm_mark_neighboring_cells_grid_v(MpmBuffers *b, const MpmReducedGrid *g, void *stream) {
+    NvtxRange nvtx_("mpm_mark_neighboring_cells_grid_v");
     int r = reduced_args_ok(b, g);
     if (r) return r;
     MPM_CHECK(mpm::launch_mark_grid_v(make_ctx(b, stream, b->cur), *g));
@@ -553,6 +578,7 @@ int mpm_mark_neighboring_cells_grid_v(MpmBuffers *b, const MpmReducedGrid *g, vo
 }
 
 int mpm_g2p_sample(MpmBuffers *b, const MpmReducedGrid *g, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_g2p_sample");
     int r = reduced_args_ok(b, g);
     if (r) return r;
     MPM_CHECK(mpm::launch_g2p_sample(make_ctx(b, stream, b->cur), *g, dt));
@@ -573,6 +599,7 @@ int64_t mpm_decoder_param_count(const MpmStressDecoder *d) {
 }
 
 int mpm_decoder_forward(const MpmStressDecoder *d, const float *rows, float *out, int64_t n, void *stream) {
+    NvtxRange nvtx_("mpm_decoder_forward");
     if (!decoder_ok(d) || n < 0 || (n > 0 && (!rows || !out))) return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_decoder_rows(*d, rows, out, n, num_sms(), static_cast<cudaStream_t>(stream)));
     return MPM_OK;
@@ -580,6 +607,7 @@ int mpm_decoder_forward(const MpmStressDecoder *d, const float *rows, float *out
 
 int mpm_decoder_stress(MpmBuffers *b, const MpmStressDecoder *d, const float *label, const float *mu,
                        void *stream) {
+    NvtxRange nvtx_("mpm_decoder_stress");
     if (!buffers_ok(b) || !decoder_ok(d) || (d->label_dim > 0 && !label) || (d->mu_dim > 0 && !mu))
         return MPM_ERR_ARG;
     MPM_CHECK(mpm::launch_decoder_stress(make_ctx(b, stream, b->cur), *d, label, mu));
