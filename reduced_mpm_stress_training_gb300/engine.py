@@ -545,8 +545,11 @@ class ReducedGrid:
         dev = engine.device
         checks = ((self.sample_index, torch.int32, None), (self.f_disp, torch.float32, n * 9),
                   (self.density, torch.float32, n))
+        def on_dev(t):
+            return t.device.type == dev.type and (dev.index is None or t.device.index == dev.index)
+
         for t, dt, numel in checks:
-            if t is None or t.device != dev or t.dtype != dt or not t.is_contiguous() or \
+            if t is None or not on_dev(t) or t.dtype != dt or not t.is_contiguous() or \
                     (numel is not None and t.numel() != numel):
                 raise ValueError("reduced substep: sample_index (int32), f_disp (n x 9) and density (n) "
                                  "must be contiguous tensors on the engine's device")

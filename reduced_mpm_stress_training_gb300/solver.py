@@ -327,10 +327,10 @@ class MPMSimulator:
             self.particle_position2obj(stem + ".obj")
         if save_visual_F:
             self.particle_F_norm2obj(dir_name + "/visualF_f_" + str(frame).zfill(10) + ".obj")
-        if include_parameter and include_parameter != "friction_angle":
-            raise ValueError(f"include_parameter {include_parameter!r}: only 'friction_angle' is defined")
         if not save_to_h5:
             return
+        if include_parameter and include_parameter != "friction_angle":
+            raise ValueError(f"include_parameter {include_parameter!r}: only 'friction_angle' is defined")
         a = self.export_frame_arrays()
         n = self.n_particles
         data = {"x": a["x"], "q": a["q"], "time": np.array([self.time]).reshape(1, 1), "masses": a["masses"],
