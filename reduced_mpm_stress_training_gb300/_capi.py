@@ -11,6 +11,7 @@ import os
 
 from . import build as _build
 
+MPM_ABI_VERSION = 3
 MPM_MAX_COLLIDERS = 8
 MPM_OK, MPM_ERR_ARG, MPM_ERR_CUDA, MPM_ERR_SIZE = 0, -1, -2, -3
 ST_OUT_OF_DOMAIN, ST_CFL, ST_NONFINITE, ST_INTERNAL, ST_BAD_INPUT = 1, 2, 4, 8, 16
@@ -185,6 +186,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
 
 
 def check_abi(lib: C.CDLL) -> None:
+    if lib.mpm_abi_version() != MPM_ABI_VERSION:
+        raise ImportError(f"libmpm_gb300 ABI version {lib.mpm_abi_version()}, binding {MPM_ABI_VERSION}: rebuild")
     out = (C.c_int64 * 6)()
     lib.mpm_struct_sizes(out)
     mine = [C.sizeof(MpmCollider), C.sizeof(MpmScene), C.sizeof(MpmPlan), C.sizeof(MpmBuffers),

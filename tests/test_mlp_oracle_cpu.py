@@ -3,7 +3,7 @@
 The oracle rounds weights, inputs and activations to bfloat16 where the
 kernels do; PyTorch here runs the same network with bf16-rounded weights in
 fp32.  The two agree to the bf16 rounding of the activations, which pins
-the oracle's forward, backward and Adam arithmetic before it judges the
+the oracle's forward, backward and Adam arithmetic before it checks the
 kernels."""
 import numpy as np
 import torch

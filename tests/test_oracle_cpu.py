@@ -1,7 +1,7 @@
 """CPU checks of the oracle itself (no GPU): closed-form known answers
 (tests/golden), an independent NumPy/LAPACK float64 restatement, and
 analytic invariants of the substep.  These pin the oracle before it is used
-to judge the GPU path."""
+to check the GPU path."""
 import json
 import os
 
