@@ -628,8 +628,9 @@ def reduced_arm(args):
     ref.F_disp[:] = rg.f_disp.reshape(n, 9).cpu().numpy()
     ref.density[:] = sc.density
     ref.sample_particle_index_short = sample
+    nt = O.max_threads()
     t0 = time.perf_counter()
-    ref.p2g2p_reduced(dt)
+    ref.p2g2p_reduced(dt, nthreads_p2g=nt)
     cpu_t = time.perf_counter() - t0
     print(json.dumps({
         "metric": "particle-substeps/s (reduced sampled-quadrature substep, 1M sand, 4096 samples, fp32)",
@@ -643,8 +644,8 @@ def reduced_arm(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src, "scope": "whole substep",
                      "alg_bytes_per_step": alg},
-        "cpu_baseline": {"value": n / cpu_t, "unit": "particle-substeps/s", "cores": 1, "kind": "port",
-                         "sample": "one reduced substep of the same state (oracle, float32)"},
+        "cpu_baseline": {"value": n / cpu_t, "unit": "particle-substeps/s", "cores": nt, "kind": "port",
+                         "sample": "one reduced substep of the same state (oracle, float32, OpenMP)"},
         "status": sim.engine.status()}), flush=True)
 
 
@@ -697,6 +698,16 @@ def decoder_arm(args):
     t_step = _events_ms(step, K) / 1e3
     sim.time += K * dt
     flops = 2 * (3 * dec.hidden + dec.mu_dim * dec.hidden + 4 * dec.hidden ** 2 + 6 * dec.hidden) * n
+    # CPU: the NumPy float32 restatement of the decoder (BLAS threads) on a 262,144-row sample
+    from oracle import decoder as OD
+
+    m_cpu = 262_144
+    rows = np.concatenate([np.tile(label.cpu().numpy(), (m_cpu, 1)), x0[:m_cpu],
+                           np.full((m_cpu, 1), sc.friction_angle, np.float32)], 1)
+    blob = dec.params.cpu().numpy()
+    t0 = time.perf_counter()
+    OD.forward(blob, rows, dec.label_dim, dec.mu_dim, dec.hidden, False, dec.omega_0, dtype=np.float32)
+    cpu_rate = m_cpu / (time.perf_counter() - t0)
     sms = torch.cuda.get_device_properties(device).multi_processor_count
     fp32_peak = sms * 128 * 2 * 2.07e9 / 1e12
     print(json.dumps({
@@ -708,7 +719,9 @@ def decoder_arm(args):
                                f"hidden {dec.hidden}, ELU",
                    "l2": "state larger than L2"},
         "decoder": {"ms": 1e3 * t_dec, "tflops": flops / t_dec / 1e12, "flops_per_particle": flops / n,
-                    "fp32_peak_nominal_tflops": fp32_peak, "frac_of_nominal": flops / t_dec / 1e12 / fp32_peak},
+                    "fp32_peak_nominal_tflops": fp32_peak, "frac_of_nominal": flops / t_dec / 1e12 / fp32_peak,
+                    "cpu_baseline": {"value": cpu_rate, "unit": "particles decoded/s", "cores": os.cpu_count(),
+                                     "kind": "port", "sample": f"{m_cpu} rows, NumPy float32 (BLAS threads)"}},
         "status": eng.status()}), flush=True)
 
 

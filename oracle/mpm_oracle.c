@@ -847,8 +847,8 @@ void PFX(update_neighboring_cells)(const OrcModel *m, int64_t ns, const int32_t 
     if (status) *status |= st;
 }
 
-/* p2g_sample_all (mpm_utils.py:353-402), sequential scatter in particle
- * order.  A particle whose base cell is marked sets F = F_disp + I, takes the
+/* p2g_sample_all (mpm_utils.py:353-402); nthreads == 1 scatters sequentially
+ * in particle order, more threads with atomics.  A particle whose base cell is marked sets F = F_disp + I, takes the
  * FCR (jelly, metal) or Drucker-Prager (sand) stress of that F with
  * J = s0 s1 s2, and scatters momentum w m v, mass w m and the force
  * dt (-(m / density) stress grad w) as three separate adds per node.  A
@@ -857,10 +857,13 @@ void PFX(update_neighboring_cells)(const OrcModel *m, int64_t ns, const int32_t 
  * flagged. */
 void PFX(p2g_sample_all)(const OrcModel *m, int64_t np, const real *x, const real *v, real *F,
                          const real *F_disp, const real *mass, const real *density, const int32_t *mask,
-                         real dt, real *gm, real *gvin, int32_t *status) {
+                         real dt, real *gm, real *gvin, int32_t *status, int nthreads) {
     const int n = m->n_grid;
     const real inv_dx = (real)m->inv_dx, mu = (real)m->mu, lam = (real)m->lam;
+    const int par = nthreads > 1;
     int st = 0;
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1) \
+    reduction(| : st) if (par)
     for (int64_t p = 0; p < np; ++p) {
         int cb[3], cell_in = 1;
         for (int d = 0; d < 3; ++d) {
@@ -898,8 +901,8 @@ void PFX(p2g_sample_all)(const OrcModel *m, int64_t np, const real *x, const rea
                     real weight = w[0][i] * w[1][j] * w[2][k];
                     int64_t g = gidx(n, base[0] + i, base[1] + j, base[2] + k);
                     real wm = weight * mp;
-                    for (int r = 0; r < 3; ++r) gvin[3 * g + r] += wm * v[3 * p + r];
-                    gm[g] += weight * mp;
+                    for (int r = 0; r < 3; ++r) add_real(&gvin[3 * g + r], wm * v[3 * p + r], par);
+                    add_real(&gm[g], weight * mp, par);
                     real dweight[3] = {dw[0][i] * w[1][j] * w[2][k] * inv_dx,
                                        w[0][i] * dw[1][j] * w[2][k] * inv_dx,
                                        w[0][i] * w[1][j] * dw[2][k] * inv_dx};
@@ -908,7 +911,7 @@ void PFX(p2g_sample_all)(const OrcModel *m, int64_t np, const real *x, const rea
                         f = f + M[r * 3 + 1] * dweight[1];
                         f = f + M[r * 3 + 2] * dweight[2];
                         f = f + (real)0; /* + body_force (zero) */
-                        gvin[3 * g + r] += dt * f;
+                        add_real(&gvin[3 * g + r], dt * f, par);
                     }
                 }
     }
@@ -924,6 +927,7 @@ void PFX(grid_normalization_and_gravity_sample_all)(const OrcModel *m, real dt, 
     const int64_t nn = (int64_t)n * n * n;
     real gdt[3];
     for (int c = 0; c < 3; ++c) gdt[c] = dt * (real)m->gravity[c];
+#pragma omp parallel for schedule(static)
     for (int64_t g = 0; g < nn; ++g)
         if (mask[g] > 0 && gm[g] > (real)1e-10f)
             for (int c = 0; c < 3; ++c) gvout[3 * g + c] = gvin[3 * g + c] / gm[g] + gdt[c];
@@ -989,7 +993,7 @@ void PFX(g2p_sample)(const OrcModel *m, int64_t ns, const int32_t *sample, int64
  * advances moving colliders and time. */
 void PFX(p2g2p_reduced)(const OrcModel *m, PFX(State) * s, int64_t np, const real *density, int64_t ns,
                         const int32_t *sample, int32_t *mask, int32_t *mask_v, const OrcCollider *cols,
-                        int ncol, double time, real dt, int32_t *status) {
+                        int ncol, double time, real dt, int nthreads_p2g, int32_t *status) {
     const int n = m->n_grid;
     const int64_t nn = (int64_t)n * n * n;
     PFX(update_x_from_u)(np, s->x0, s->u, s->x);
@@ -998,7 +1002,7 @@ void PFX(p2g2p_reduced)(const OrcModel *m, PFX(State) * s, int64_t np, const rea
     memset(mask_v, 0, (size_t)nn * sizeof(int32_t));
     PFX(update_neighboring_cells)(m, ns, sample, np, s->x, 2, mask, status);
     PFX(p2g_sample_all)(m, np, s->x, s->v, s->F, s->F_disp, s->mass, density, mask, dt, s->grid_m,
-                        s->grid_v_in, status);
+                        s->grid_v_in, status, nthreads_p2g);
     PFX(grid_normalization_and_gravity_sample_all)(m, dt, mask, s->grid_m, s->grid_v_in, s->grid_v_out);
     for (int k = 0; k < ncol; ++k) {
         if (cols[k].kind == 0) PFX(collide_surface)(m, &cols[k], time, s->grid_v_out);

@@ -340,7 +340,7 @@ class OracleSim:
         idx = np.ascontiguousarray(self.sample_particle_index_short, dtype=np.int32).reshape(-1)
         return idx, C.c_int64(idx.shape[0])
 
-    def p2g2p_reduced(self, dt: float) -> None:
+    def p2g2p_reduced(self, dt: float, nthreads_p2g: int = 1) -> None:
         """p2g2p_reduced (mpm_solver_warp.py:214-227): the grid of the sampled
         particles' neighbourhood; particles are not moved (time += dt)."""
         s = self._state()
@@ -351,7 +351,7 @@ class OracleSim:
         self._fn("p2g2p_reduced")(C.byref(self.model), C.byref(s), C.c_int64(self.n), _ptr(self.density), ns,
                                   _ptr(idx), _ptr(self.neighboring_cells), _ptr(self.neighboring_cells_grid_v),
                                   arr, C.c_int(ncol), C.c_double(self.time), self._real(dt),
-                                  C.byref(self.status))
+                                  C.c_int(nthreads_p2g), C.byref(self.status))
         for col in self.colliders:
             advance_collider(col, self.time, dt)
         self.time = self.time + dt

@@ -169,3 +169,16 @@ def test_bad_sample_index_is_flagged():
     sim.p2g2p_reduced(sc.dt)
     assert sim.status.value & O.ST_BAD_INPUT
     assert not sim.neighboring_cells.any() and not sim.grid_m.any()
+
+
+def test_parallel_reduced_p2g_matches_serial():
+    out = []
+    for nt in (1, 4):
+        sc, sim = _sim("sand", fdisp_sigma=0.05, bits=64)
+        sim.sample_particle_index_short = np.array([7, 120, 300, 301], np.int32)
+        sim.p2g2p_reduced(sc.dt, nthreads_p2g=nt)
+        out.append(sim)
+    a, b = out
+    assert np.array_equal(a.neighboring_cells, b.neighboring_cells)
+    for f in ("grid_m", "grid_v_in", "grid_v_out"):
+        assert np.abs(getattr(a, f) - getattr(b, f)).max() <= 1e-12 * np.abs(getattr(a, f)).max(), f
