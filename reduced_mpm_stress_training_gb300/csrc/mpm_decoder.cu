@@ -137,7 +137,10 @@ __device__ __forceinline__ void dec_tail(const float *sm, const DecLayout &L, fl
         const float *W = sm + L.wh + l * HP * HP;
         const float *b = sm + L.bh + l * HP;
         float g[HP];
-#pragma unroll
+        // the 64-wide form keeps one output row per iteration (g in local memory): a full
+        // unroll of 64 x 64 multiply-adds costs minutes of compile time
+        constexpr int kJUnroll = HP <= 32 ? HP : 1;
+#pragma unroll kJUnroll
         for (int j = 0; j < HP; ++j) {
             float acc = b[j];
             const float4 *w4 = reinterpret_cast<const float4 *>(W + j * HP);
