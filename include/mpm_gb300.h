@@ -17,6 +17,11 @@
  * Physics faults (particles leaving the grid, CFL violation, non-finite
  * F or stress) never trap: kernels OR a bit into the device status word
  * (MpmBuffers.status) which the caller reads when it likes.
+ * State the library keeps itself: the last CUDA error text (per host
+ * thread), the SM count per device, two copy lanes (a side stream and
+ * events each, created by the first host-buffer transfer), the 16 MiB
+ * device array of mpm_p2g2p_noalloc, and a once-per-device shared-memory
+ * opt-in of the decoder kernels.
  */
 #ifndef MPM_GB300_H
 #define MPM_GB300_H
