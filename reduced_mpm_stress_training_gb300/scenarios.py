@@ -84,6 +84,38 @@ class Scene:
         return out
 
 
+def scene_to_dict(sc: Scene) -> dict:
+    """A scene as plain JSON-ready values (tuples become lists)."""
+    return {k: (list(v) if isinstance(v, tuple) else v) for k, v in dataclasses.asdict(sc).items()}
+
+
+def scene_from_dict(d: dict) -> Scene:
+    """The inverse of scene_to_dict; unknown keys raise TypeError."""
+    kw = dict(d)
+    for k in ("box_lo", "box_hi", "gravity", "v0"):
+        if k in kw and kw[k] is not None:
+            kw[k] = tuple(float(x) for x in kw[k])
+    return Scene(**kw)
+
+
+def save_scenes(path: str, scenes) -> None:
+    """One scene or a list of scenes to a JSON file."""
+    import json
+
+    data = [scene_to_dict(s) for s in scenes] if isinstance(scenes, (list, tuple)) else scene_to_dict(scenes)
+    with open(path, "w") as f:
+        json.dump(data, f, indent=1)
+
+
+def load_scenes(path: str):
+    """A scene (or list of scenes) from a JSON file written by save_scenes."""
+    import json
+
+    with open(path) as f:
+        data = json.load(f)
+    return [scene_from_dict(d) for d in data] if isinstance(data, list) else scene_from_dict(data)
+
+
 def sand_column_32k(seed: int = 0) -> Scene:
     return Scene("sand_column_32k", 32768, 64, 1.0, (0.4, 0.4, 0.05), (0.6, 0.6, 0.65), "sand",
                  2e5, 0.3, 30.0, 2200.0, (0.0, 0.0, -9.8), 1e-4, 200, seed=seed)

@@ -57,3 +57,19 @@ def test_obj_lines_match_the_reference_format():
     pts = np.array([[0.5, 0.25, 0.125], [1.0 / 3.0, 0.1, 2.0]], np.float32)
     text = FR.obj_lines(pts, [(0.0, 0.0, 0.0), (np.float32(0.5), 0, 0)])
     assert text == "v 0.5 0.25 0.125 0.0 0.0 0.0\nv 0.33333334 0.1 2.0 0.5 0 0\n"
+
+
+def test_scene_json_round_trip(tmp_path):
+    from reduced_mpm_stress_training_gb300 import scenarios as S
+
+    scenes = S.batch_64(n_scenes=5) + [S.sand_column_1m(), S.metal_block_1m()]
+    path = str(tmp_path / "scenes.json")
+    S.save_scenes(path, scenes)
+    back = S.load_scenes(path)
+    assert back == scenes
+    x_back, x_orig = back[0].particles()[0], scenes[0].particles()[0]   # same seeded particles
+    assert np.array_equal(x_back, x_orig)
+    S.save_scenes(path, scenes[0])
+    assert S.load_scenes(path) == scenes[0]
+    with pytest.raises(TypeError):
+        S.scene_from_dict(dict(S.scene_to_dict(scenes[0]), unknown=1))
