@@ -11,6 +11,8 @@ the reference, written out independently of the oracle's code.
                        :45-52), metal (:59-84, :36-43), jelly (:29-34)
   kat_p2g.json         one particle's P2G contributions to its 27 nodes
                        (engine_stress/mpm_utils.py:190-227)
+  kat_reduced_p2g.json one particle's reduced-substep P2G with a diagonal F_disp
+                       (engine_stress/mpm_utils.py:353-402, stresses :29-34, :45-52)
 
 Run:  python tests/golden/make_golden.py
 """
@@ -151,9 +153,55 @@ def make_p2g():
                 nodes=nodes)
 
 
+def make_reduced_p2g():
+    """One particle through p2g_sample_all (engine_stress/mpm_utils.py:353-402) with a
+    diagonal F_disp, so F = I + F_disp is its own SVD and the stress is closed-form:
+    FCR for jelly and metal (:29-34, R = I, J = s0 s1 s2), Drucker-Prager for sand
+    (:45-52, U diag(c) V^T F^T = diag(c_i s_i)).  No affine term; the force uses the
+    volume m / density.  Per-node (mass, momentum) after the three adds."""
+    n, lim = 16, 1.0
+    inv_dx = n / lim
+    x = [0.4137, 0.5261, 0.3319]
+    v = [0.3, -0.2, 0.1]
+    fdisp = [0.02, -0.03, 0.01]
+    m, rho, dt = 2.0e-4, 2000.0, 1e-4
+    base, fx = [], []
+    for d in range(3):
+        gp = x[d] * inv_dx
+        b = int(gp - 0.5)
+        base.append(b)
+        fx.append(gp - b)
+    w = [[0.5 * (1.5 - f) ** 2, 0.75 - (f - 1.0) ** 2, 0.5 * (f - 0.5) ** 2] for f in fx]
+    dw = [[f - 1.5, -2.0 * (f - 1.0), f - 0.5] for f in fx]
+    sig = [1.0 + f for f in fdisp]
+    out = []
+    for material, E, nu in (("jelly", 2e5, 0.3), ("metal", 1e7, 0.3), ("sand", 2e5, 0.3)):
+        mu, lam = lame(E, nu)
+        if material == "sand":
+            ls = sum(math.log(s) for s in sig)
+            tau = [(2 * mu * math.log(s) + lam * ls) / s * s for s in sig]
+        else:
+            J = sig[0] * sig[1] * sig[2]
+            tau = [2 * mu * (s - 1.0) * s + lam * J * (J - 1.0) for s in sig]
+        nodes = []
+        for i in range(3):
+            for j in range(3):
+                for k in range(3):
+                    wt = w[0][i] * w[1][j] * w[2][k]
+                    gw = [dw[0][i] * w[1][j] * w[2][k] * inv_dx, w[0][i] * dw[1][j] * w[2][k] * inv_dx,
+                          w[0][i] * w[1][j] * dw[2][k] * inv_dx]
+                    mom = [wt * m * v[r] + dt * (-(m / rho) * tau[r] * gw[r]) for r in range(3)]
+                    nodes.append(dict(index=[base[0] + i, base[1] + j, base[2] + k], mass=wt * m, momentum=mom))
+        out.append(dict(material=material, E=E, nu=nu, n_grid=n, grid_lim=lim, x=x, v=v, F_disp=diag9(fdisp),
+                        mass=m, density=rho, dt=dt, stress=diag9(tau), nodes=nodes))
+    return out
+
+
 if __name__ == "__main__":
+    with open(os.path.join(HERE, "kat_reduced_p2g.json"), "w") as f:
+        json.dump(make_reduced_p2g(), f, indent=1)
     with open(os.path.join(HERE, "kat_return_map.json"), "w") as f:
         json.dump(make_return_map(), f, indent=1)
     with open(os.path.join(HERE, "kat_p2g.json"), "w") as f:
         json.dump(make_p2g(), f, indent=1)
-    print("wrote kat_return_map.json, kat_p2g.json")
+    print("wrote kat_return_map.json, kat_p2g.json, kat_reduced_p2g.json")
