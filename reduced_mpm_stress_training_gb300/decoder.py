@@ -30,15 +30,15 @@ from . import _capi as A
 _HIDDEN = ("dec1", "dec2", "dec3", "dec4")
 
 
-def _strip(sd: dict) -> dict:
+def _strip(sd: dict, dtype=torch.float32) -> dict:
     if any(k.startswith("decoder.") for k in sd):
         sd = {k[len("decoder."):]: v for k, v in sd.items() if k.startswith("decoder.")}
-    return {k: torch.as_tensor(v).detach().to("cpu", torch.float32) for k, v in sd.items()}
+    return {k: torch.as_tensor(v, dtype=dtype).detach().to("cpu") for k, v in sd.items()}
 
 
-def pack(sd: dict, siren: bool) -> torch.Tensor:
-    """NetDec state dict -> the packed float32 blob (CPU)."""
-    sd = _strip(sd)
+def pack(sd: dict, siren: bool, dtype=torch.float32) -> torch.Tensor:
+    """NetDec state dict -> the packed blob (CPU; float32 is what the kernels take)."""
+    sd = _strip(sd, dtype)
     prep = ("prepare.min_x_torch", "prepare.max_x_torch") if siren else \
         ("prepare.mean_x_torch", "prepare.std_x_torch")
     parts = [sd["dec0.weight"], sd["dec0.bias"]]

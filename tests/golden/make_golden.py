@@ -13,6 +13,9 @@ the reference, written out independently of the oracle's code.
                        (engine_stress/mpm_utils.py:190-227)
   kat_reduced_p2g.json one particle's reduced-substep P2G with a diagonal F_disp
                        (engine_stress/mpm_utils.py:353-402, stresses :29-34, :45-52)
+  kat_decoder.json     the stress decoder NetDec with hand-set weights on four rows,
+                       ELU and SIREN (offline_training_xhat_and_stress_and_mu/
+                       CROMnet_secondary.py:203-301, 447-525)
 
 Run:  python tests/golden/make_golden.py
 """
@@ -197,11 +200,66 @@ def make_reduced_p2g():
     return out
 
 
+def make_decoder():
+    """NetDec (offline_training_xhat_and_stress_and_mu/CROMnet_secondary.py:203-301) with
+    small hand-set weights, evaluated with plain math: Prepare (standardise, or clip to
+    [-1, 1] with SIREN; :507-525), five Linear + activation (ELU / sin(30 x); :447-463),
+    Linear to 6, mean_q + q * std_q (:476-477).  label 2, mu 1, hidden 3."""
+    lbl, mu_dim, h = 2, 1, 3
+    n_in = lbl + 3 + mu_dim
+
+    def lin(W, b, x):
+        return [b[j] + sum(W[j][k] * x[k] for k in range(len(x))) for j in range(len(W))]
+
+    sd = {"dec0.weight": [[0.1 * (j + 1) - 0.05 * k for k in range(n_in)] for j in range(h)],
+          "dec0.bias": [0.01 * j for j in range(h)]}
+    for l, name in enumerate(("dec1", "dec2", "dec3", "dec4")):
+        sd[name + ".weight"] = [[((j + k + l) % 3 - 1) * 0.5 for k in range(h)] for j in range(h)]
+        sd[name + ".bias"] = [-0.1 + 0.05 * l + 0.02 * j for j in range(h)]
+    sd["enc.weight"] = [[0.2 * (c - k) for k in range(h)] for c in range(6)]
+    sd["enc.bias"] = [float(c) for c in range(6)]
+    sd["invStandardizeQ.mean_q_torch"] = [1.0, 2.0, 3.0, 4.0, 5.0, 6.0]
+    sd["invStandardizeQ.std_q_torch"] = [2.0, 0.5, 1.0, 3.0, 0.25, 1.5]
+    rows = [[0.3, -1.2, 0.45, 0.52, 0.31, 30.0], [-0.7, 0.1, 0.61, 0.38, 0.75, 25.0],
+            [1.5, 0.4, 0.40, 0.50, 0.10, 35.0], [0.0, 0.0, 0.55, 0.45, 0.60, 20.0]]
+    out = []
+    for siren in (False, True):
+        d = dict(sd)
+        if siren:
+            d["prepare.min_x_torch"], d["prepare.max_x_torch"] = [0.35, 0.35, 0.05], [0.65, 0.65, 0.85]
+        else:
+            d["prepare.mean_x_torch"], d["prepare.std_x_torch"] = [0.5, 0.5, 0.45], [0.25, 0.5, 1.0]
+        q_all = []
+        for r in rows:
+            x = list(r)
+            for c in range(3):
+                if siren:
+                    lo, hi = d["prepare.min_x_torch"][c], d["prepare.max_x_torch"][c]
+                    x[lbl + c] = 2 * (r[lbl + c] - lo) / (hi - lo) - 1
+                else:
+                    x[lbl + c] = (r[lbl + c] - d["prepare.mean_x_torch"][c]) / d["prepare.std_x_torch"][c]
+
+            def act(z):
+                return math.sin(30.0 * z) if siren else (z if z > 0 else math.expm1(z))
+
+            y = [act(z) for z in lin(d["dec0.weight"], d["dec0.bias"], x)]
+            for name in ("dec1", "dec2", "dec3", "dec4"):
+                y = [act(z) for z in lin(d[name + ".weight"], d[name + ".bias"], y)]
+            q = lin(d["enc.weight"], d["enc.bias"], y)
+            q_all.append([d["invStandardizeQ.mean_q_torch"][c] + q[c] * d["invStandardizeQ.std_q_torch"][c]
+                          for c in range(6)])
+        out.append(dict(siren=siren, omega_0=30.0, label_dim=lbl, mu_dim=mu_dim, hidden=h, state_dict=d,
+                        rows=rows, q=q_all))
+    return out
+
+
 if __name__ == "__main__":
+    with open(os.path.join(HERE, "kat_decoder.json"), "w") as f:
+        json.dump(make_decoder(), f, indent=1)
     with open(os.path.join(HERE, "kat_reduced_p2g.json"), "w") as f:
         json.dump(make_reduced_p2g(), f, indent=1)
     with open(os.path.join(HERE, "kat_return_map.json"), "w") as f:
         json.dump(make_return_map(), f, indent=1)
     with open(os.path.join(HERE, "kat_p2g.json"), "w") as f:
         json.dump(make_p2g(), f, indent=1)
-    print("wrote kat_return_map.json, kat_p2g.json, kat_reduced_p2g.json")
+    print("wrote kat_return_map.json, kat_p2g.json, kat_reduced_p2g.json, kat_decoder.json")

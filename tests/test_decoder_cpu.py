@@ -72,3 +72,24 @@ def test_library_parameter_count(built):
         assert lib.mpm_decoder_param_count(C.byref(d)) == D.pack(sd, case["siren"]).numel()
     bad = A.MpmStressDecoder(0, 6, 1, 65, 0, 30.0, 0)   # wider than the kernels take
     assert lib.mpm_decoder_param_count(C.byref(bad)) < 0
+
+
+@pytest.mark.parametrize("siren", [False, True])
+def test_decoder_golden(siren):
+    """tests/golden/kat_decoder.json (hand-set weights, plain-math evaluation) against
+    the packing + NumPy restatement and the PyTorch float32 restatement."""
+    import json
+    import os
+
+    cases = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "kat_decoder.json")))
+    g = next(c for c in cases if c["siren"] == siren)
+    want = np.array(g["q"])
+    # the packing and the restatement, in float64 on the fixture's exact values
+    blob = D.pack(g["state_dict"], siren, dtype=torch.float64).numpy()
+    q64 = OD.forward(blob, np.array(g["rows"]), g["label_dim"], g["mu_dim"], g["hidden"], siren, g["omega_0"])
+    assert np.abs(q64 - want).max() <= 1e-9 * np.abs(want).max()
+    if not siren:  # float32 weights and rows: ELU is well conditioned (sin(30 x) of inputs near 30 is not)
+        sd = {k: torch.tensor(v, dtype=torch.float32) for k, v in g["state_dict"].items()}
+        q32 = netdec_torch(sd, torch.tensor(g["rows"], dtype=torch.float32), g["label_dim"], siren,
+                           g["omega_0"]).numpy()
+        assert np.abs(q32 - want).max() <= 1e-5 * np.abs(want).max()
