@@ -48,6 +48,20 @@ from .engine import (Collider, MPMEngine, MPMStatusError, ReducedGrid, ScenePara
                      material_code, dp_alpha)
 
 
+def flatten2nD(index, shape_tuple):
+    """Module helper of the reference (engine_stress/mpm_solver_warp.py:14-22): the
+    C-order multi-index of flat position ``index`` in an array of shape ``shape_tuple``
+    (the first component is not bounded by the first extent, as there)."""
+    out, rest = [], int(index)
+    for d in range(len(shape_tuple)):
+        stride = 1
+        for e in shape_tuple[d + 1:]:
+            stride *= int(e)
+        q, rest = divmod(rest, stride)
+        out.append(q)
+    return out
+
+
 class _Model:
     """Readable mirror of MPMModelStruct (engine_stress/warp_utils.py:61-81)."""
 
@@ -486,4 +500,4 @@ class MPMSimulator:
 
 MPM_Simulator_WARP = MPMSimulator
 
-__all__ = ["MPMSimulator", "MPM_Simulator_WARP", "MPMStatusError"]
+__all__ = ["MPMSimulator", "MPM_Simulator_WARP", "MPMStatusError", "flatten2nD"]
