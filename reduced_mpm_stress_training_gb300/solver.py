@@ -16,6 +16,9 @@ the current PyTorch CUDA stream.  Differences a caller can see:
   works as before.
 * ``initialize`` starts from F = I (the reference leaves F = 0 until
   ``load_from_sampling`` sets it to I, :149).
+* ``mpm_state.particle_F_trial`` is not kept (it lives only inside G2P);
+  ``particle_Jp`` and ``particle_external_force``, which the reference
+  allocates and never writes, read as zeros.
 * Extensions: ``set_parameters(E=, nu=, gravity=(gx,gy,gz), particle_vol=)``,
   ``load_vol_from_tensor``, ``load_F_from_tensor``, ``load_yield_from_tensor``.
 * All the reference's colliders are built.  Moving ones advance on the
@@ -112,6 +115,12 @@ class _State:
             return sim._density
         if name == "sample_particle_index_short":
             return sim._sample_index
+        if name in ("particle_Jp", "particle_external_force"):  # allocated, never written (:63-65)
+            shape = (n,) if name == "particle_Jp" else (n, 3)
+            return torch.zeros(shape, dtype=torch.float32, device=sim.device)
+        if name == "particle_F_trial":
+            raise AttributeError("particle_F_trial is not kept: F_trial lives only inside G2P, which "
+                                 "stores the return-mapped F (particle_F)")
         if name in ("neighboring_cells", "neighboring_cells_grid_v"):
             return getattr(sim._reduced_grid(), name)
         if name in ("grid_m", "grid_v_in", "grid_v_out"):
