@@ -245,3 +245,26 @@ def test_oracle_extended_colliders_known_answers():
     assert tuple(col.point) == tuple(float(f(a + 1e-4 * b)) for a, b in zip((0.5, 0.5, 0.5), (1.0, -2.0, 0.5)))
     with pytest.raises(ValueError):
         O.rotating_disk((0.5, 0.5, 0.5), (0.05, 1.0, 0.0), 0.3, 0.07, 4.0)
+
+
+def test_injected_faults_set_status_bits():
+    """Failure detection on the host: a NaN position freezes its particle and sets
+    the out-of-domain bit, a NaN deformation gradient sets the non-finite bit, an
+    exploding velocity sets the CFL bit -- status words, never a trap or a hang."""
+    sc = S.small_column(256, 16)
+    m = O.make_model(sc.n_grid, material="sand", E=sc.E, nu=sc.nu, gravity=sc.gravity)
+    x0, v0, vol, mass = sc.particles()
+    x_nan = x0.copy()
+    x_nan[5] = np.nan
+    sim = O.OracleSim(m, x_nan, mass, vol, v0, bits=32)
+    sim.p2g2p(sc.dt)
+    assert sim.status.value & O.ST_OUT_OF_DOMAIN
+    sim = O.OracleSim(m, x0, mass, vol, v0, bits=32)
+    sim.F[7] = np.nan
+    sim.p2g2p(sc.dt)
+    assert sim.status.value & O.ST_NONFINITE
+    v_fast = v0.copy()
+    v_fast[3] = (0.0, 0.0, 1e4)   # far beyond dx / dt
+    sim = O.OracleSim(m, x0, mass, vol, v_fast, bits=32)
+    sim.p2g2p(sc.dt)
+    assert sim.status.value & O.ST_CFL
