@@ -112,3 +112,38 @@ def test_surface_collider_normalises_and_rejects_sticky_friction():
         Collider.surface((0, 0, 0), (0, 1, 0), "sticky", 0.5)
     assert Collider.surface((0, 0, 0), (0, 1, 0), "slip").surface_type == 1
     assert Collider.surface((0, 0, 0), (0, 1, 0), "separate", 0.3).surface_type == 2
+
+
+def test_plain_c_caller(built, tmp_path):
+    """The header compiles as strict C99 and a C program links the library and plans
+    buffers through it, agreeing with the ctypes binding (host-only calls)."""
+    import os
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.dirname(A.lib_path())
+    exe = str(tmp_path / "c_abi_plan")
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-pedantic", "-I", os.path.join(root, "include"),
+                    os.path.join(root, "tests", "c_abi_plan.c"), "-L", libdir, "-lmpm_gb300",
+                    "-Wl,-rpath," + libdir, "-o", exe], check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split("\n")
+    abi = out[0].split()
+    assert int(abi[1]) == 3
+    assert [int(x) for x in abi[3:]] == [C.sizeof(A.MpmCollider), C.sizeof(A.MpmScene), C.sizeof(A.MpmPlan),
+                                         C.sizeof(A.MpmBuffers), C.sizeof(A.MpmReducedGrid),
+                                         C.sizeof(A.MpmStressDecoder)]
+    from reduced_mpm_stress_training_gb300.engine import SceneParams
+
+    lib = A.load()
+    table = (A.MpmScene * 1)()
+    table[0] = SceneParams(n_particles=1024, n_grid=32, grid_lim=1.0, material=A.SAND, mu=1.0, lam=1.0,
+                           friction_angle=30.0, gravity=(0.0, 0.0, 0.0)).to_struct(0)
+    plan = A.MpmPlan()
+    assert lib.mpm_plan(table, 1, 1024, 0, C.byref(plan)) == 0
+    got = [int(x) for x in out[1].split()[1:]]
+    assert got == [plan.state_bytes, plan.workspace_bytes, plan.total_blocks, plan.particle_stride, plan.chunk_size]
+    assert out[2].split() == ["bad", str(A.MPM_ERR_ARG)]
