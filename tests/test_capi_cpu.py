@@ -147,3 +147,22 @@ def test_plain_c_caller(built, tmp_path):
     got = [int(x) for x in out[1].split()[1:]]
     assert got == [plan.state_bytes, plan.workspace_bytes, plan.total_blocks, plan.particle_stride, plan.chunk_size]
     assert out[2].split() == ["bad", str(A.MPM_ERR_ARG)]
+
+
+def test_c_example_compiles_and_links(built, tmp_path):
+    """A complete C caller of the substep (tests/c_abi_substep.c) compiles as C99
+    against the header and the CUDA runtime and links the library."""
+    import os
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    if cc is None or not os.path.exists(os.path.join(cuda, "include", "cuda_runtime.h")):
+        pytest.skip("no C compiler or CUDA runtime headers")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.dirname(A.lib_path())
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(root, "include"),
+                    "-I", os.path.join(cuda, "include"), os.path.join(root, "tests", "c_abi_substep.c"),
+                    "-L", libdir, "-lmpm_gb300", "-L", os.path.join(cuda, "lib64"), "-lcudart", "-lm",
+                    "-Wl,-rpath," + libdir, "-o", str(tmp_path / "c_abi_substep")], check=True)
