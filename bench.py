@@ -15,6 +15,9 @@ One JSON line on rank 0.  A "step" is one substep of every particle.
             loads u, v, stress from pinned host memory (load_uvstress_from_tensor),
             runs the substep and reads u, v, F_disp, stress back to pinned host
             memory (export_uvFstress_from_warp)
+  extra keys of the default line (skipped with --no-extras / --no-adjoint /
+            --no-surrogate): metal_block_1m, reduced_1m, decoder_1m, batch_64,
+            adjoint, surrogate -- each also runs alone with --workload
   --workload reduced_1m -- the reduced sampled-quadrature substep
             (p2g2p_reduced) on the same column with 4,096 sample points
   --workload decoder_1m -- the substep with the reference's stress decoder
@@ -53,6 +56,17 @@ def workload_config(sc, world: int) -> dict:
 KERNEL_BYTES = {"p2g": 116, "g2p": 192}  # algorithmic particle bytes per launch unit
 
 
+def timing_label(K: int, gsize: int, repeats: int) -> str:
+    """What the timed region ran, in words."""
+    parts = []
+    if K // gsize:
+        parts.append(f"{K // gsize} replay(s) of a CUDA graph of {gsize} substeps")
+    if K % gsize:
+        parts.append(f"{K % gsize} eager substep(s)")
+    return (f"{repeats} x {K} substeps ({' + '.join(parts)}), CUDA events on the launching stream, "
+            "max over ranks")
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -63,6 +77,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint measurement")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-stress measurement")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the metal, reduced, decoder and batched workloads in the default line")
     return ap.parse_args()
 
 
@@ -346,6 +362,9 @@ def reference_arm(args, sc, world, rank):
         "warmup": args.warmup, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(sc, args.gpus),
+        "l2": "not applicable (host cores)",
+        "timing": {"method": f"{args.steps} substeps of the bounded sample, wall clock (perf_counter)",
+                   "repeats": 1, "substeps_timed": done, "timed_region_s": round(el, 4)},
         "cpu_baseline": {"value": rate, "unit": "particle-substeps/s", "cores": nt, "kind": "port",
                          "sample": f"first {n_sample} particles of the seeded {sc.n_particles}-particle "
                                    f"column on the {sc.n_grid}^3 grid, one substep per step "
@@ -377,22 +396,33 @@ def gb300_arm(args, sc, world, rank, local):
     torch.cuda.synchronize()
     sim.check_status()
 
-    gsize = 32
+    K = args.steps
+    gsize = max(1, min(32, K))
     graph = eng.graph(gsize, float(sim.time), dt)
     graph.replay()  # untimed: the first replay uploads the graph
     torch.cuda.synchronize()
     st = torch.cuda.current_stream()
-    K = args.steps
+
+    def k_substeps():
+        # exactly K substeps: K // gsize graph replays, the remainder eagerly
+        for _ in range(K // gsize):
+            graph.replay()
+        for _ in range(K % gsize):
+            eng.substep_raw(float(sim.time), dt)
+
+    # the timed region repeats the K-substep block R times so it lasts at least
+    # half a second (the clock sampler then sees several samples under load)
+    t_block = _events_ms(k_substeps, 1) / 1e3
+    repeats = max(1, min(1000, math.ceil(0.5 / max(t_block, 1e-6))))
+    repeats = int(max_over_ranks(float(repeats), world, device))
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(device.index if world == 1 else local)
     barrier(world, device)
     torch.cuda.synchronize()
     clocks.start()
     ev0.record(st)
-    for _ in range(K // gsize):
-        graph.replay()
-    for _ in range(K % gsize):
-        eng.substep_raw(float(sim.time), dt)
+    for _ in range(repeats):
+        k_substeps()
     ev1.record(st)
     torch.cuda.synchronize()
     barrier(world, device)
@@ -401,8 +431,9 @@ def gb300_arm(args, sc, world, rank, local):
     t_max = max_over_ranks(t, world, device)
     status = eng.status()
     launches_per_substep = 6  # scan_tiles, scan_finish, scatter, p2g, grid, g2p
-    value = world * n * K / t_max
-    ms_per_step = 1e3 * t_max / K
+    timed_substeps = repeats * K
+    value = world * n * timed_substeps / t_max
+    ms_per_step = 1e3 * t_max / timed_substeps
 
     # per-stage times, eager, CUDA events on the launching stream
     stage_ms = {"sort": 0.0, "p2g": 0.0, "grid": 0.0, "g2p": 0.0}
@@ -456,7 +487,7 @@ def gb300_arm(args, sc, world, rank, local):
         return
     peak, peak_src = measured_peak_hbm()
     alg = ALG_BYTES[sc.material]
-    achieved = alg * n / (t_max / K) / 1e9
+    achieved = alg * n / (t_max / timed_substeps) / 1e9
     traffic = profiled_traffic(sc.name)
     kern = {}
     for kname, b in KERNEL_BYTES.items():
@@ -472,10 +503,10 @@ def gb300_arm(args, sc, world, rank, local):
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform particles in the column; reference sampling data absent)",
-        "config": dict(workload_config(sc, world),
-                       l2="state larger than L2 (2 x %.0f MB particle buffers + grid); no flush"
-                          % (eng.plan.state_bytes / 1e6),
-                       timing=f"CUDA graph of {gsize} substeps replayed, CUDA events"),
+        "config": workload_config(sc, world),
+        "l2": "state larger than L2 (2 x %.0f MB particle buffers + grid); no flush" % (eng.plan.state_bytes / 1e6),
+        "timing": {"method": timing_label(K, gsize, repeats), "repeats": repeats,
+                   "substeps_timed": timed_substeps, "timed_region_s": round(t_max, 4)},
         "roofline": {"bound": "hbm", "kernel": "substep (sort + p2g + grid + g2p)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
@@ -486,10 +517,18 @@ def gb300_arm(args, sc, world, rank, local):
         "roofline_kernels": kern,
         "e2e": {"value": e2e_value, "unit": "particle-substeps/s", "h2d_bytes_per_step": 60 * n,
                 "d2h_bytes_per_step": 96 * n, "steps": k_e2e},
-        "gpu_launches": int(round(K * launches_per_substep)),
+        "gpu_launches": int(round(timed_substeps * launches_per_substep)),
         "clocks": clk,
         "status": status,
     }
+    if world == 1 and not args.no_extras:
+        # the other workloads, recorded in the same line; one failing keeps the headline
+        for key, fn in (("metal_block_1m", metal_result), ("reduced_1m", reduced_result),
+                        ("decoder_1m", decoder_result), ("batch_64", batched_result)):
+            try:
+                line[key] = fn(args, device)
+            except Exception as exc:  # noqa: BLE001
+                line[key] = {"error": repr(exc)}
     if not args.no_adjoint:
         line["adjoint"] = adjoint_extra(device)
     if not args.no_surrogate:
@@ -503,50 +542,101 @@ def gb300_arm(args, sc, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
-def batched_arm(args):
-    """64 scenes (sand and metal, N log-uniform in [1e4, 2e5], grids 48/64/96) in one
-    batched launch per stage, against the same scenes stepped one by one."""
+def metal_result(args, device) -> dict:
+    """The von Mises metal block variant of the large column: 1,048,576 particles,
+    128^3 grid, E = 1e7, yield stress 1e5, density 2700, v0 = (0, 0, -1), dt 5e-5;
+    substeps replayed from a CUDA graph (CUDA events) after a warm-up."""
     import torch
 
-    import __graft_entry__ as g
+    from reduced_mpm_stress_training_gb300 import scenarios as S
+
+    sc = S.metal_block_1m()
+    sim = S.build_simulator(sc, device=device)
+    eng = sim.engine
+    for k in range(max(3, args.warmup)):
+        sim.p2g2p(k, sc.dt)
+    sim.check_status()
+    gsize = 32
+    graph = eng.graph(gsize, float(sim.time), sc.dt)
+    graph.replay()
+    reps = 8
+    t = _events_ms(graph.replay, reps) / 1e3 / gsize
+    n = sc.n_particles
+    peak, peak_src = measured_peak_hbm()
+    achieved = ALG_BYTES["metal"] * n / t / 1e9
+    return {"metric": "particle-substeps/s (1M von Mises metal, fp32)", "value": n / t,
+            "unit": "particle-substeps/s", "ms_per_step": 1e3 * t, "steps": reps * gsize,
+            "timing": f"{reps} replays of a CUDA graph of {gsize} substeps, CUDA events",
+            "config": workload_config(sc, 1),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "algorithmic_bytes_per_unit": ALG_BYTES["metal"],
+                         "peak_source": peak_src},
+            "status": eng.status()}
+
+
+def batched_result(args, device) -> dict:
+    """64 scenes (sand and metal, N log-uniform in [1e4, 2e5], grids 48/64/96) in one
+    batched launch per stage, replayed from a CUDA graph, over the workload's full 500
+    substeps (warm-up and graph upload included), against the same scenes stepped one
+    by one.  The status word and the finiteness of every scene are checked at the end."""
+    import torch
+
+    from reduced_mpm_stress_training_gb300 import _capi as A
     from reduced_mpm_stress_training_gb300 import scenarios as S
     from reduced_mpm_stress_training_gb300.batched import BatchedMPM, time_chunk_size
 
-    g.build()
     scenes = S.batch_64()
-    device = torch.device("cuda:0")
     b = BatchedMPM(scenes, device=device, chunk_size="auto")
     dt = scenes[0].dt
-    for _ in range(max(3, args.warmup)):
+    total = scenes[0].substeps
+    W = max(3, args.warmup)
+    for _ in range(W):
         b.step(dt)
     gsize = 32
     graph = b.graph(gsize, dt)
     graph.replay()
     torch.cuda.synchronize()
+    done = W + gsize
+    K = (total - done) // gsize * gsize
     st = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # the workload is defined for scenes[0].substeps substeps (500): warm-up plus the
-    # timed replays stay within it (later, some stiff metal scenes leave the CFL bound)
-    K = max(gsize, args.steps - args.steps % gsize)
-    K = max(gsize, min(K, (scenes[0].substeps - max(3, args.warmup) - gsize) // gsize * gsize))
     e0.record(st)
     for _ in range(K // gsize):
         graph.replay()
     e1.record(st)
     torch.cuda.synchronize()
+    done += K
+    for _ in range(total - done):
+        b.step(dt)
+    torch.cuda.synchronize()
     t = e0.elapsed_time(e1) / 1e3 / K
+    finite = bool(torch.isfinite(b.engine.export(A.FIELD_U)).all()) and bool(
+        torch.isfinite(b.engine.export(A.FIELD_STRESS)).all())
     seq = sum(time_chunk_size([s], b.chunk_size, device, steps=16) for s in scenes)
     n = b.n_particles
-    print(json.dumps({"metric": "particle-substeps/s (64-scene batch, fp32)", "value": n / t,
-                      "unit": "particle-substeps/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
-                      "ms_per_step": 1e3 * t, "higher_is_better": True, "dtype": "f32",
-                      "data": "synthetic", "config": {"workload": "batch_64", "scenes": len(scenes),
-                                                      "particles": n, "chunk_size": b.chunk_size},
-                      "one_by_one": {"value": n / seq, "ms_per_step": 1e3 * seq},
-                      "speedup_vs_one_by_one": seq / t, "status": b.engine.status()}), flush=True)
+    return {"metric": "particle-substeps/s (64-scene batch, fp32)", "value": n / t,
+            "unit": "particle-substeps/s", "steps": K, "warmup": W, "ms_per_step": 1e3 * t,
+            "substeps_run": total, "timing": f"{K // gsize} replays of a CUDA graph of {gsize} substeps of all "
+                                              "64 scenes, CUDA events",
+            "config": {"workload": "batch_64: 64 scenes, N log-uniform [1e4, 2e5], grids 48/64/96, 25 % metal "
+                                   "(E log-uniform [1e5, 1e6]), dt 1e-4, 500 substeps",
+                       "scenes": len(scenes), "particles": n, "chunk_size": b.chunk_size},
+            "one_by_one": {"value": n / seq, "ms_per_step": 1e3 * seq},
+            "speedup_vs_one_by_one": seq / t, "status": b.engine.status(), "finite_after_500": finite}
 
 
-def reduced_arm(args):
+def batched_arm(args):
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    d = batched_result(args, torch.device("cuda:0"))
+    d.update(n_gpus=1, higher_is_better=True, dtype="f32", data="synthetic")
+    print(json.dumps(d), flush=True)
+
+
+def reduced_result(args, device) -> dict:
     """The reduced sampled-quadrature substep (MPM_Simulator_WARP.p2g2p_reduced) on the
     large sand column after two plain substeps, with 4,096 seeded sample points:
     every particle is scanned, the marked ones scatter, and the dense 128^3 grid is
@@ -556,15 +646,12 @@ def reduced_arm(args):
     import numpy as np
     import torch
 
-    import __graft_entry__ as g
     from reduced_mpm_stress_training_gb300 import MPM_Simulator_WARP
     from reduced_mpm_stress_training_gb300 import _capi as A
     from reduced_mpm_stress_training_gb300 import scenarios as S
 
-    g.build()
     sc = S.sand_column_1m()
     n, ng, dt = sc.n_particles, sc.n_grid, sc.dt
-    device = torch.device("cuda:0")
     x0, v0, vol, mass = sc.particles()
     sim = MPM_Simulator_WARP(n, n_grid=ng, grid_lim=sc.grid_lim, device=device)
     sim.set_parameters(material=sc.material, E=sc.E, nu=sc.nu, friction_angle=sc.friction_angle,
@@ -632,7 +719,7 @@ def reduced_arm(args):
     t0 = time.perf_counter()
     ref.p2g2p_reduced(dt, nthreads_p2g=nt)
     cpu_t = time.perf_counter() - t0
-    print(json.dumps({
+    return {
         "metric": "particle-substeps/s (reduced sampled-quadrature substep, 1M sand, 4096 samples, fp32)",
         "value": n / t, "unit": "particle-substeps/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
         "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -646,10 +733,19 @@ def reduced_arm(args):
                      "alg_bytes_per_step": alg},
         "cpu_baseline": {"value": n / cpu_t, "unit": "particle-substeps/s", "cores": nt, "kind": "port",
                          "sample": "one reduced substep of the same state (oracle, float32, OpenMP)"},
-        "status": sim.engine.status()}), flush=True)
+        "status": sim.engine.status()}
 
 
-def decoder_arm(args):
+def reduced_arm(args):
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    print(json.dumps(reduced_result(args, torch.device("cuda:0"))), flush=True)
+
+
+def decoder_result(args, device) -> dict:
     """The reduced-order loop's substep with the reference's stress decoder as the
     stress source (NetDec 10 -> 30 x 5 -> 6, ELU, seeded reference initialisation):
     each step decodes every particle's stress into the state (mpm_decoder_stress)
@@ -657,15 +753,12 @@ def decoder_arm(args):
     import numpy as np
     import torch
 
-    import __graft_entry__ as g
     from reduced_mpm_stress_training_gb300 import MPM_Simulator_WARP
     from reduced_mpm_stress_training_gb300 import scenarios as S
     from reduced_mpm_stress_training_gb300.decoder import StressDecoder
 
-    g.build()
     sc = S.sand_column_1m()
     n, dt = sc.n_particles, sc.dt
-    device = torch.device("cuda:0")
     x0, v0, vol, mass = sc.particles()
     sim = MPM_Simulator_WARP(n, n_grid=sc.n_grid, grid_lim=sc.grid_lim, device=device)
     sim.set_parameters(material=sc.material, E=sc.E, nu=sc.nu, friction_angle=sc.friction_angle,
@@ -710,7 +803,7 @@ def decoder_arm(args):
     cpu_rate = m_cpu / (time.perf_counter() - t0)
     sms = torch.cuda.get_device_properties(device).multi_processor_count
     fp32_peak = sms * 128 * 2 * 2.07e9 / 1e12
-    print(json.dumps({
+    return {
         "metric": "particle-substeps/s (decoded-stress substep: NetDec stress + p2g2p, 1M sand, fp32)",
         "value": n / t_step, "unit": "particle-substeps/s", "n_gpus": 1, "steps": K, "warmup": args.warmup,
         "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -722,7 +815,16 @@ def decoder_arm(args):
                     "fp32_peak_nominal_tflops": fp32_peak, "frac_of_nominal": flops / t_dec / 1e12 / fp32_peak,
                     "cpu_baseline": {"value": cpu_rate, "unit": "particles decoded/s", "cores": os.cpu_count(),
                                      "kind": "port", "sample": f"{m_cpu} rows, NumPy float32 (BLAS threads)"}},
-        "status": eng.status()}), flush=True)
+        "status": eng.status()}
+
+
+def decoder_arm(args):
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    print(json.dumps(decoder_result(args, torch.device("cuda:0"))), flush=True)
 
 
 def main():

@@ -258,8 +258,10 @@ int mpm_export_grid(MpmBuffers *b, int32_t scene, float *grid_m, float *grid_v_i
  * device memory for its own pool, or code that runs where cudaMalloc is not
  * allowed: b->workspace is ignored (may be NULL) and the scratch lives in one
  * library-owned 16 MiB device array (held by every GPU that loads the
- * library).  Returns MPM_ERR_SIZE if b->plan.workspace_bytes exceeds 16 MiB
- * (a 64^3 grid with 32,768 particles fits).  All calls share that array: each
+ * library).  Returns MPM_ERR_SIZE if the substep's part of the workspace
+ * (everything in b->plan.workspace_bytes but the host-transfer staging, which
+ * this call never uses) exceeds 16 MiB: a 64^3 grid fits with up to about a
+ * million particles, a 128^3 grid does not.  All calls share that array: each
  * call clears it and re-sorts from the particle positions, and calls that
  * overlap on the GPU race.  The first call on a device looks up the array's
  * address (cudaGetSymbolAddress); make it before any stream capture.  Never

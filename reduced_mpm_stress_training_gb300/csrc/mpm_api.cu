@@ -91,6 +91,10 @@ WsLayout ws_layout(const MpmPlan &p) {
 
 }  // namespace
 
+namespace mpm {
+int record_cuda_error(cudaError_t e) { return fail_cuda(e); }
+}  // namespace mpm
+
 // bytes at the start of the workspace that a substep touches: everything
 // but the host-transfer staging and the slot-of-uid table, which come last
 int64_t mpm::substep_workspace_bytes(const MpmPlan &p) { return ws_layout(p).staging; }

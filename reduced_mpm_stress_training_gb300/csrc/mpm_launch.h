@@ -88,4 +88,7 @@ cudaError_t launch_g2p_sample(const Ctx &cx, const MpmReducedGrid &g, float dt);
 
 int field_components(int field);
 
+// records e for mpm_last_cuda_error() (as every entry point does) and returns MPM_ERR_CUDA
+int record_cuda_error(cudaError_t e);
+
 }  // namespace mpm

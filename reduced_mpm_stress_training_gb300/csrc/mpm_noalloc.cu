@@ -48,7 +48,7 @@ void *noalloc_workspace(int *err) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev < 0 || dev >= 64) {
-        *err = MPM_ERR_CUDA;
+        *err = mpm::record_cuda_error(e != cudaSuccess ? e : cudaErrorInvalidDevice);
         return nullptr;
     }
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
@@ -56,7 +56,7 @@ void *noalloc_workspace(int *err) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_workspace);
         if (e != cudaSuccess || !p) {
-            *err = MPM_ERR_CUDA;
+            *err = mpm::record_cuda_error(e != cudaSuccess ? e : cudaErrorInvalidSymbol);
             return nullptr;
         }
         g_noalloc_ptr[dev] = p;
@@ -76,7 +76,7 @@ extern "C" int mpm_p2g2p_noalloc(MpmBuffers *b, float time, float dt, void *stre
     // the array holds whatever the last call left: start from a cleared
     // workspace and keys recomputed from the positions
     cudaError_t e = cudaMemsetAsync(ws, 0, (size_t)need, static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) return MPM_ERR_CUDA;
+    if (e != cudaSuccess) return mpm::record_cuda_error(e);
     MpmBuffers local = *b;
     local.workspace = ws;
     local.keys_valid = 0;

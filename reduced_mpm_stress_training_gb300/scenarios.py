@@ -14,6 +14,7 @@ Scenes (sizes as named):
   metal_block_1m       same column, von Mises metal E=1e7, yield 1e5, rho 2700, v0=(0,0,-1)
   sand_rollout_131k    131,072 sand particles, 96^3 grid, dt 1e-4, 100 substeps, v0 ~ N(0, 0.1^2)
   batch_64             64 scenes, N log-uniform [1e4, 2e5], grid 48/64/96, 25 % metal
+                       (metal E log-uniform [1e5, 1e6] like the sand, yield [5e4, 5e5])
 """
 from __future__ import annotations
 
@@ -159,8 +160,12 @@ def batch_64(seed: int = 0, n_scenes: int = 64) -> list[Scene]:
         ng = int(rng.choice([48, 64, 96]))
         metal = rng.random() < 0.25
         if metal:
+            # the workload fixes the metal's yield stress range, not its E: it takes the
+            # sand's E range, which keeps dt 1e-4 inside the elastic-wave CFL bound on a
+            # 96^3 grid (E = 1e7 at 2700 kg/m^3 does not, and goes non-finite)
+            E = float(math.exp(rng.uniform(math.log(1e5), math.log(1e6))))
             sc = Scene(f"batch_{s}_metal", n, ng, 1.0, (0.35, 0.35, 0.1), (0.65, 0.65, 0.7),
-                       "metal", 1e7, 0.3, 30.0, 2700.0, (0.0, 0.0, -9.8), 1e-4, 500,
+                       "metal", E, 0.3, 30.0, 2700.0, (0.0, 0.0, -9.8), 1e-4, 500,
                        yield_stress=float(math.exp(rng.uniform(math.log(5e4), math.log(5e5)))),
                        seed=seed * 1000 + s)
         else:
