@@ -244,6 +244,20 @@ int mpm_p2g(MpmBuffers *b, float dt, void *stream); /* mpm_utils.py:190-227 */
 int mpm_grid_update(MpmBuffers *b, float time, float dt, void *stream); /* :229-237 + colliders */
 int mpm_g2p(MpmBuffers *b, float dt, void *stream); /* mpm_utils.py:241-306, :4-19 */
 
+/* No counterpart in the reference (its P2G, engine_stress/mpm_utils.py:190-227,
+ * adds with float atomics in whatever order threads run, as mpm_p2g does).
+ * The P2G stage with sums that do not depend on the order in which warps
+ * run: each cell's particles are taken in uid order and the per-block node
+ * tiles are summed per node in a fixed order, so the whole substep (with
+ * mpm_sort, mpm_grid_update, mpm_g2p) is a deterministic function of its
+ * inputs -- what finite-difference checks of gradients need.  Same results
+ * as mpm_p2g up to float32 rounding.  `scratch`: caller-owned device memory
+ * of mpm_p2g_ordered_bytes(&plan) bytes (a 6x6x6 float4 tile per grid block
+ * plus a block index).  mpm_p2g2p_ordered is the substep with it. */
+int64_t mpm_p2g_ordered_bytes(const MpmPlan *plan);
+int mpm_p2g_ordered(MpmBuffers *b, void *scratch, float dt, void *stream);
+int mpm_p2g2p_ordered(MpmBuffers *b, void *scratch, float time, float dt, void *stream);
+
 /* Dense (n,n,n) C-order copy of one scene's grid after the last stage that
  * wrote it: grid_m and grid_v_in (momentum) are valid between mpm_p2g and
  * mpm_grid_update, grid_v_out after mpm_grid_update.  Untouched nodes read 0,

@@ -112,6 +112,9 @@ _SIGS = {
     "mpm_export_frame": ([C.POINTER(MpmBuffers), C.c_void_p, C.c_void_p], C.c_int),
     "mpm_p2g2p": ([C.POINTER(MpmBuffers), C.c_float, C.c_float, C.c_void_p], C.c_int),
     "mpm_sort": ([C.POINTER(MpmBuffers), C.c_void_p], C.c_int),
+    "mpm_p2g_ordered_bytes": ([C.POINTER(MpmPlan)], C.c_int64),
+    "mpm_p2g_ordered": ([C.POINTER(MpmBuffers), C.c_void_p, C.c_float, C.c_void_p], C.c_int),
+    "mpm_p2g2p_ordered": ([C.POINTER(MpmBuffers), C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "mpm_p2g": ([C.POINTER(MpmBuffers), C.c_float, C.c_void_p], C.c_int),
     "mpm_grid_update": ([C.POINTER(MpmBuffers), C.c_float, C.c_float, C.c_void_p], C.c_int),
     "mpm_g2p": ([C.POINTER(MpmBuffers), C.c_float, C.c_void_p], C.c_int),

@@ -43,12 +43,15 @@ class SandRollout:
 
     def __init__(self, scene: Scene, n_substeps: int | None = None, checkpoint_every: int = 10,
                  device="cuda:0", chunk_size: int = 128, particles=None, initial: dict | None = None,
-                 grid_tape: bool = True):
+                 grid_tape: bool = True, ordered: bool = True):
         """particles: (x0, v0, vol, mass) arrays overriding the scene's sampling;
         initial: {field id: (n, comps) tensor} loaded after them (e.g. a
         prestrained F with its stress); grid_tape: keep every substep's grid
         from the forward pass (n_substeps x mpm_substep_grid_bytes of device
-        memory) so the backward pass recomputes states by G2P alone."""
+        memory) so the backward pass recomputes states by G2P alone; ordered:
+        P2G sums in a fixed order (mpm_p2g_ordered), so the forward is a
+        deterministic function of (v0, E, friction angle) and finite
+        differences of it are meaningful at small steps."""
         if scene.material != "sand":
             raise ValueError("the adjoint covers sand (Drucker-Prager) scenes only")
         if checkpoint_every < 1:
@@ -60,6 +63,7 @@ class SandRollout:
         self.device = torch.device(device)
         self.params = scene_params(scene)
         self.engine = MPMEngine([self.params], device=self.device, chunk_size=chunk_size)
+        self.engine.ordered = bool(ordered)
         self.lib = self.engine.lib
         x0, v0, vol, mass = scene.particles() if particles is None else particles
         self.n = x0.shape[0]

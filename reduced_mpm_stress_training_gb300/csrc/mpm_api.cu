@@ -433,6 +433,27 @@ int mpm_g2p(MpmBuffers *b, float dt, void *stream) {
     return MPM_OK;
 }
 
+int64_t mpm_p2g_ordered_bytes(const MpmPlan *plan) {
+    if (!plan || plan->total_blocks < 0) return -1;
+    return mpm::ordered_scratch_bytes(plan->total_blocks);
+}
+
+int mpm_p2g_ordered(MpmBuffers *b, void *scratch, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_p2g_ordered");
+    if (!buffers_ok(b) || !scratch) return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_p2g_ordered(make_ctx(b, stream, b->cur), dt, scratch));
+    return MPM_OK;
+}
+
+int mpm_p2g2p_ordered(MpmBuffers *b, void *scratch, float time, float dt, void *stream) {
+    NvtxRange nvtx_("mpm_p2g2p_ordered");
+    int r = mpm_sort(b, stream);
+    if (r) return r;
+    if ((r = mpm_p2g_ordered(b, scratch, dt, stream))) return r;
+    if ((r = mpm_grid_update(b, time, dt, stream))) return r;
+    return mpm_g2p(b, dt, stream);
+}
+
 int mpm_p2g2p(MpmBuffers *b, float time, float dt, void *stream) {
     NvtxRange nvtx_("mpm_p2g2p");
     int r = mpm_sort(b, stream);

@@ -26,7 +26,13 @@ cudaError_t launch_keys(const Ctx &cx);
 cudaError_t launch_sort(const Ctx &cx);
 
 // transfer stages (mpm_substep.cu)
-cudaError_t launch_p2g(const Ctx &cx, float dt);
+// partials / blk_index non-null: the ordered mode (see launch_p2g_ordered)
+cudaError_t launch_p2g(const Ctx &cx, float dt, float4 *partials = nullptr, int *blk_index = nullptr);
+// P2G whose sums do not depend on the order in which warps run (mpm_ordered.cu):
+// each cell's particles in uid order, per-block tiles to `scratch`, summed per
+// node in a fixed order into grid_acc.  scratch: ordered_scratch_bytes
+int64_t ordered_scratch_bytes(int64_t total_blocks);
+cudaError_t launch_p2g_ordered(const Ctx &cx, float dt, void *scratch);
 cudaError_t launch_grid(const Ctx &cx, float time, float dt);
 // defer_stress: store F_trial as F and skip the return map (surrogate stage follows)
 cudaError_t launch_g2p(const Ctx &cx, float dt, bool defer_stress = false);

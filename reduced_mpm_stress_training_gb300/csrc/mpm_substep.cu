@@ -254,9 +254,14 @@ __device__ __forceinline__ bool p2g_next_round(int &rem0, int &rem1, int &pos0, 
     return true;
 }
 
+// partials == nullptr: the tile is flushed with float4 atomics into grid_acc.
+// Otherwise (the ordered mode of mpm_p2g_ordered) the whole 6x6x6 tile of
+// work-list entry bi goes to partials[bi] and blk_index[block] = bi; the
+// gather kernel then sums the <= 8 tiles covering each node in a fixed order.
 __global__ void __launch_bounds__(kP2GWarps * 32, 2) p2g_kernel(const MpmScene *__restrict__ scenes,
                                                                 int n_scenes, PState st, Ws ws, float dt,
-                                                                int *status) {
+                                                                int *status, float4 *partials,
+                                                                int *blk_index) {
     extern __shared__ __align__(16) unsigned char p2g_smem_raw[];
     P2GWarpSmem *smem = reinterpret_cast<P2GWarpSmem *>(p2g_smem_raw);
     const unsigned full = 0xffffffffu;
@@ -346,9 +351,16 @@ __global__ void __launch_bounds__(kP2GWarps * 32, 2) p2g_kernel(const MpmScene *
         }
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         if (bad) atomicOr(status, MPM_ST_INTERNAL);
-        // flush the tile: one float4 atomic per non-zero node
         const int nb = S.n_blocks_axis;
-        for (int i = lane; i < kP2GSlots; i += 32) {
+        if (partials) {
+            // ordered mode: the whole tile to this entry's slot, in node order
+            float4 *dst = partials + (int64_t)bi * kTileNodes;
+            for (int i = lane; i < kTileNodes; i += 32)
+                dst[i] = sm.tile[p2g_slot(i / (kTile * kTile), (i / kTile) % kTile, i % kTile)];
+            if (lane == 0) blk_index[be.x] = bi;
+        }
+        // flush the tile: one float4 atomic per non-zero node
+        for (int i = lane; i < kP2GSlots && !partials; i += 32) {
             const float4 a = sm.tile[i];
             if (a.x != 0.0f || a.y != 0.0f || a.z != 0.0f || a.w != 0.0f) {
                 const int tx = i / (kTile * kRowSlots), ty = (i / kRowSlots) % kTile;
@@ -689,14 +701,21 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
             }
         }
         warp_histogram(ws.counts, ws.cell_counts, key);
+        // every warp is done with buffer `buf` (the next iteration prefetches into it)
         __syncthreads();
-        if (ch.w >= 0) {  // the chunk's records are contiguous in `out`: coalesced write-out
-            const int nq = min(ch.z, ws.n - ch.y) * kRecQuads;
-            float4 *dst = out.rec + (int64_t)ch.y * kRecQuads;
-            for (int l = threadIdx.x; l < nq; l += CH)
-                dst[l] = sm.outrec[(l / kRecQuads) * kOutStride + (l % kRecQuads)];
+        if (ch.w >= 0) {
+            // each warp writes its own 32 records (contiguous in `out`) with coalesced
+            // float4 stores
+            const int w0 = (int)(threadIdx.x & ~31u);
+            const int np = min(min(32, ch.z - w0), ws.n - ch.y - w0);
+            const int nq = np > 0 ? np * kRecQuads : 0;
+            float4 *dst = out.rec + (int64_t)(ch.y + w0) * kRecQuads;
+            const float4 *src = sm.outrec + w0 * kOutStride;
+            for (int l = (int)(threadIdx.x & 31u); l < nq; l += 32)
+                dst[l] = src[(l / kRecQuads) * kOutStride + (l % kRecQuads)];
         }
-        __syncthreads();  // buffer `buf` and outrec are refilled by the next iteration
+        // outrec is rewritten only after the next iteration's barrier, which
+        // every warp reaches after its write-out
         c = cn; ch = chn; slot = slotn;
         cn = cnn; chn = chnn; slotn = slotnn;
         buf ^= 1;
@@ -726,7 +745,7 @@ static int persistent_grid(const Ctx &cx, int per_sm) {
     return g < cx.ws.max_chunks ? g : (cx.ws.max_chunks > 0 ? cx.ws.max_chunks : 1);
 }
 
-cudaError_t launch_p2g(const Ctx &cx, float dt) {
+cudaError_t launch_p2g(const Ctx &cx, float dt, float4 *partials, int *blk_index) {
     // more than the 48 KB of static shared memory: opt in once per device
     static bool attr_set[64] = {false};
     const int bytes = (int)(sizeof(P2GWarpSmem) * kP2GWarps);
@@ -745,7 +764,7 @@ cudaError_t launch_p2g(const Ctx &cx, float dt) {
     int grid = (int)(want < (int64_t)cx.num_sms * 32 ? want : (int64_t)cx.num_sms * 32);
     if (grid < 1) grid = 1;
     p2g_kernel<<<grid, kP2GWarps * 32, bytes, cx.stream>>>(cx.scenes, cx.n_scenes, cx.st, cx.ws, dt,
-                                                           cx.status);
+                                                           cx.status, partials, blk_index);
     return cudaGetLastError();
 }
 

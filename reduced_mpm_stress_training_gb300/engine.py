@@ -225,6 +225,7 @@ class MPMEngine:
         self.on_error = "raise"
         self._pending = None
         self.surrogate = None
+        self._ordered_scratch = None
         self._allocate(fresh=True)
 
     # ------------------------------------------------------------------ layout
@@ -274,6 +275,9 @@ class MPMEngine:
             A.check(self.lib.mpm_init(C.byref(b), self.stream), "mpm_init")
         else:
             b.keys_valid = 0  # block keys depend on the grid
+        if self._ordered_scratch is not None:  # sized by the plan's grid blocks
+            self._ordered_scratch = None
+            self.ordered = True
 
     def _sync_moving_colliders(self) -> None:
         """Moving colliders advance on the device (mpm_grid_update); copy their
@@ -393,9 +397,27 @@ class MPMEngine:
             surrogate.bind(self)
         self.surrogate = surrogate
 
+    @property
+    def ordered(self) -> bool:
+        """True: substeps use the ordered P2G (mpm_p2g2p_ordered), whose sums do
+        not depend on the order in which warps run, so a run is a deterministic
+        function of its inputs (finite-difference gradient checks need that)."""
+        return self._ordered_scratch is not None
+
+    @ordered.setter
+    def ordered(self, on: bool) -> None:
+        if on and self._ordered_scratch is None:
+            nbytes = int(self.lib.mpm_p2g_ordered_bytes(C.byref(self.plan)))
+            self._ordered_scratch = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        elif not on:
+            self._ordered_scratch = None
+
     def _p2g2p(self, time: float, dt: float) -> None:
         sur = self.surrogate
-        if sur is None:
+        if sur is None and self._ordered_scratch is not None:
+            A.check(self.lib.mpm_p2g2p_ordered(C.byref(self.buf), self._ordered_scratch.data_ptr(), time, dt,
+                                               self.stream), "mpm_p2g2p_ordered")
+        elif sur is None:
             A.check(self.lib.mpm_p2g2p(C.byref(self.buf), time, dt, self.stream), "mpm_p2g2p")
         else:
             A.check(self.lib.mpm_p2g2p_surrogate(C.byref(self.buf), sur.params_ptr(), C.byref(sur.cfg),
@@ -421,6 +443,8 @@ class MPMEngine:
         s = self.stream
         if name == "sort":
             A.check(self.lib.mpm_sort(b, s), "mpm_sort")
+        elif name == "p2g" and self._ordered_scratch is not None:
+            A.check(self.lib.mpm_p2g_ordered(b, self._ordered_scratch.data_ptr(), dt, s), "mpm_p2g_ordered")
         elif name == "p2g":
             A.check(self.lib.mpm_p2g(b, dt, s), "mpm_p2g")
         elif name == "grid":

@@ -208,13 +208,40 @@ def test_sand_column_32k_rollout(cuda):
     errs64 = compare(sim, ref64)
     spread = {f: rel(getattr(ref, f), getattr(ref64, f)) for f in ("v", "C", "F", "stress")}
     print("gpu vs oracle32", errs, "gpu vs oracle64", errs64, "oracle32 vs oracle64", spread)
-    assert errs["x"] < TOL_ROLLOUT and errs["F"] < TOL_ROLLOUT
+    assert errs["x"] < TOL_ROLLOUT and errs["F"] < TOL_ROLLOUT and errs["v"] < TOL_ROLLOUT
     g = gpu_state(sim)
     for f in ("stress",):
         ok, info = within_fp32_floor(g[f], getattr(ref, f), getattr(ref64, f), rtol=TOL_ROLLOUT)
         assert ok, (f, info)
     g = sim.mpm_state.particle_x.cpu().numpy()
     assert rel(g, ref.x0 + ref.u) < TOL_ROLLOUT
+
+
+def test_metal_block_32k_rollout(cuda):
+    """A von Mises metal block (E = 1e7, yield stress 1e5, rho 2700, v0 =
+    (0, 0, -1), hardening with xi = 0.1) of 32,768 particles on the 64^3
+    grid, dropped on the sticky floor: 200 substeps at dt 1e-4 against the
+    oracle, x, v and F within the 1e-4 rollout bar, the hardened yield
+    stresses within 1e-5 (engine_stress/mpm_utils.py:59-84, :36-43)."""
+    sc = S.Scene("metal_block_32k", 32768, 64, 1.0, (0.4, 0.4, 0.05), (0.6, 0.6, 0.65), "metal", 1e7, 0.3,
+                 30.0, 2700.0, (0.0, 0.0, -9.8), 1e-4, 200, yield_stress=1e5, hardening=1, xi=0.1,
+                 v0=(0.0, 0.0, -1.0), seed=3)
+    sim = gpu_sim(sc)
+    ref = oracle_sim(sc)
+    ref64 = oracle_sim(sc, bits=64)
+    for k in range(sc.substeps):
+        sim.p2g2p(k, sc.dt)
+        ref.p2g2p(sc.dt)
+        ref64.p2g2p(sc.dt)
+    assert sim.check_status() == 0
+    errs = compare(sim, ref, fields=("x", "v", "F"))
+    errs64 = compare(sim, ref64, fields=("x", "v", "F"))
+    spread = {f: rel(getattr(ref, f), getattr(ref64, f)) for f in ("v", "F")}
+    print("gpu vs oracle32", errs, "gpu vs oracle64", errs64, "oracle32 vs oracle64", spread)
+    assert all(e < TOL_ROLLOUT for e in errs.values()), errs
+    g = gpu_state(sim)
+    assert rel(g["yield_"].ravel(), ref.yield_) < TOL_STEP
+    assert (g["yield_"].ravel() > sc.yield_stress * (1 + 1e-6)).sum() > 100  # the impact hardened the block
 
 
 def test_out_of_domain_particle_is_flagged_not_fatal(cuda):
@@ -297,7 +324,7 @@ def _dev_norm_and_trace(tau):
 def test_full_size_workload(cuda, name):
     """The 1,048,576-particle, 128^3 workloads at full size and full length.
 
-    5 substeps in lockstep with the float32 oracle at the per-substep
+    20 substeps in lockstep with the float32 oracle at the per-substep
     tolerance, then the rest of the 1,000 substeps on the GPU alone, checked
     through properties that hold at any size: no status bits, finite state,
     every particle inside the domain, the returned stress inside the yield
@@ -308,14 +335,14 @@ def test_full_size_workload(cuda, name):
     sim = gpu_sim(sc)
     ref = oracle_sim(sc)
     ref64 = oracle_sim(sc, bits=64)
-    lockstep = 5
+    lockstep = 20
     for k in range(lockstep):
         sim.p2g2p(k, sc.dt)
         ref.p2g2p(sc.dt)
         ref64.p2g2p(sc.dt)
-    errs = compare(sim, ref, fields=("x", "v", "F"))
-    tol = _step_tol(ref, ref64, errs)
-    assert all(errs[f] < tol[f] for f in errs), (errs, tol)
+        errs = compare(sim, ref, fields=("x", "v", "F"))
+        tol = _step_tol(ref, ref64, errs)
+        assert all(errs[f] < tol[f] for f in errs), (k, errs, tol)
     g = gpu_state(sim)
     ok, info = within_fp32_floor(g["stress"], ref.stress, ref64.stress)
     assert ok, info
