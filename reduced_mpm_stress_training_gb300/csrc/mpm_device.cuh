@@ -513,6 +513,108 @@ __device__ __forceinline__ bool sand_return_map_spectral(const MpmScene &S, cons
 }
 
 // ---------------------------------------------------------------------------
+// von Mises return map + StVK-Hencky stress without an SVD
+// (von_mises_return_mapping, engine_stress/mpm_utils.py:59-84, then
+// kirchoff_stress_StVK on the returned F, :36-43 via :301-302).  With
+// e_i = log s_i and h = e - tr(e)/3 (E = log(b)/2 as a matrix, b = F F^T):
+//   plastic iff |2 mu h| > yield;  r = dgamma / (|h| + 1e-6),
+//   dgamma = |h| + 1e-6 - yield / (2 mu)   (the reference's 1e-6 included)
+//   F = exp(-r dev E) F_trial  (= U exp(e - r h) V^T), else F = F_trial
+//   tau = U diag(2 mu e' + lam tr e') V^T = T R,  T = 2 mu E' + lam tr(E) I,
+//   R = U V^T = b^{-1/2} F_trial (the polar rotation, unchanged by the return)
+// so everything is a function of b evaluated in Newton form (as for sand),
+// plus R.  Returns false (SVD path) for inverted or extremely compressed
+// elements, where the reference's 0.01 clamp of the singular values matters.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool metal_return_map_spectral(const MpmScene &S, const float Ft[9], float &yld,
+                                                          float Fo[9], float tau[9]) {
+    const float J = Ft[0] * (Ft[4] * Ft[8] - Ft[5] * Ft[7]) - Ft[1] * (Ft[3] * Ft[8] - Ft[5] * Ft[6]) +
+                    Ft[2] * (Ft[3] * Ft[7] - Ft[4] * Ft[6]);
+    if (!(J > 0.0f)) return false;
+    float B[6], ev[3];
+    left_strain(Ft, B);
+    sym_eig3(B, ev);
+    if (!(ev[2] > -0.99f)) return false;  // smallest singular value below 0.1
+    const float mu = S.mu, lam = S.lam;
+    const float e0 = 0.5f * log1pf(ev[0]), e1 = 0.5f * log1pf(ev[1]), e2 = 0.5f * log1pf(ev[2]);
+    const float tr = e0 + e1 + e2;
+    const float h0 = e0 - tr / 3.0f, h1 = e1 - tr / 3.0f, h2 = e2 - tr / 3.0f;
+    const float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2);
+    Newton3 N;
+    newton3_setup(B, ev, N);
+    const float q0 = 1.0f + ev[0], q1 = 1.0f + ev[1], q2 = 1.0f + ev[2];
+    // R = b^{-1/2} F_trial: s(beta) = (1 + beta)^{-1/2}
+    const float s0 = rsqrtf(q0), s1 = rsqrtf(q1), s2 = rsqrtf(q2);
+    float Sm[6], R[9];
+    newton3_eval(N, s0, s2, -s0 * s1 / (q0 * s0 + q1 * s1), -s1 * s2 / (q1 * s1 + q2 * s2), Sm);
+    sym_times(Sm, Ft, R);
+    const float l01 = 0.5f * log_ratio_div(q0, q1), l12 = 0.5f * log_ratio_div(q1, q2);
+    float E[6];
+    newton3_eval(N, e0, e2, l01, l12, E);
+    float T[6];
+    if (2.0f * mu * hn > yld) {
+        const float hn_eps = hn + 1e-6f;
+        const float dg = hn_eps - yld / (2.0f * mu);
+        const float r = dg / hn_eps;
+        const float g0 = expf(-r * h0), g1 = expf(-r * h1), g2 = expf(-r * h2);
+        const float z01 = -r * l01, z12 = -r * l12;
+        const float dg01 = g1 * z01 * expm1_div(z01 * (ev[0] - ev[1]));
+        const float dg12 = g2 * z12 * expm1_div(z12 * (ev[1] - ev[2]));
+        float Gm[6];
+        newton3_eval(N, g0, g2, dg01, dg12, Gm);
+        sym_times(Gm, Ft, Fo);
+        const float k1 = 1.0f - r, k0 = r * tr / 3.0f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float id = (k == 0 || k == 3 || k == 5) ? 1.0f : 0.0f;
+            T[k] = 2.0f * mu * (k1 * E[k] + k0 * id) + lam * tr * id;
+        }
+        if (S.hardening == 1) yld = yld + 2.0f * mu * S.xi * dg;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fo[k] = Ft[k];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) T[k] = 2.0f * mu * E[k] + ((k == 0 || k == 3 || k == 5) ? lam * tr : 0.0f);
+    }
+    sym_times(T, R, tau);
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Fixed-corotated stress without an SVD (kirchoff_stress_FCR,
+// engine_stress/mpm_utils.py:29-34, jelly, F = F_trial):
+//   tau = 2 mu (F - R) F^T + lam J (J - 1) I,   R = U V^T,
+// and (F - R) F^T = b - b^{1/2} = f(B), f(beta) = (1 + beta) - sqrt(1 + beta)
+// = sqrt(1 + beta) beta / (1 + sqrt(1 + beta)),  f[x, y] = 1 - 1 / (sqrt(1 + x)
+// + sqrt(1 + y)): accurate as B -> 0.  J = det F as in the reference.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool jelly_stress_spectral(const MpmScene &S, const float Ft[9], float Fo[9],
+                                                      float tau[9]) {
+    const float J = Ft[0] * (Ft[4] * Ft[8] - Ft[5] * Ft[7]) - Ft[1] * (Ft[3] * Ft[8] - Ft[5] * Ft[6]) +
+                    Ft[2] * (Ft[3] * Ft[7] - Ft[4] * Ft[6]);
+    if (!(J > 0.0f)) return false;
+    float B[6], ev[3];
+    left_strain(Ft, B);
+    sym_eig3(B, ev);
+    if (!(ev[2] > -0.99f)) return false;
+    Newton3 N;
+    newton3_setup(B, ev, N);
+    const float r0 = sqrtf(1.0f + ev[0]), r1 = sqrtf(1.0f + ev[1]), r2 = sqrtf(1.0f + ev[2]);
+    const float f0 = r0 * ev[0] / (1.0f + r0), f2 = r2 * ev[2] / (1.0f + r2);
+    const float d01 = 1.0f - 1.0f / (r0 + r1), d12 = 1.0f - 1.0f / (r1 + r2);
+    float Fm[6];
+    newton3_eval(N, f0, f2, d01, d12, Fm);
+    const float dia = S.lam * J * (J - 1.0f);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Fo[k] = Ft[k];
+    float T[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) T[k] = 2.0f * S.mu * Fm[k] + ((k == 0 || k == 3 || k == 5) ? dia : 0.0f);
+    sym_full(T, tau);
+    return true;
+}
+
+// ---------------------------------------------------------------------------
 // Return mapping + Kirchhoff stress for one particle, fused on ONE SVD.
 // The reference (g2p_apic_and_stress, engine_stress/mpm_utils.py:284-306)
 // takes a second SVD of the returned F for the stress.  The returned F is
@@ -524,6 +626,8 @@ __device__ __forceinline__ bool sand_return_map_spectral(const MpmScene &S, cons
 __device__ __forceinline__ void return_map_stress(const MpmScene &S, const float Ft[9], float &yld,
                                                   float Fo[9], float tau[9]) {
     if (S.material == MPM_SAND && sand_return_map_spectral(S, Ft, Fo, tau)) return;
+    if (S.material == MPM_METAL && metal_return_map_spectral(S, Ft, yld, Fo, tau)) return;
+    if (S.material == MPM_JELLY && jelly_stress_spectral(S, Ft, Fo, tau)) return;
     Svd d;
     svd3(Ft, d);
     const float mu = S.mu, lam = S.lam;

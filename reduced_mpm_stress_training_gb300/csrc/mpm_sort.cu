@@ -124,13 +124,20 @@ __global__ void __launch_bounds__(256) scan_tiles_kernel(Ws ws) {
 }
 
 // Phase 2: bucket offsets / cursors, the G2P chunk list and the P2G block
-// list; zeroes the histogram for the next substep.
+// list; zeroes the histogram for the next substep.  Each thread first finds
+// the offsets of its buckets (a CTA scan on top of the tile's exclusive
+// prefix); then the CTA's warps take its non-empty buckets one at a time and
+// write the 64 cell offsets of each with a warp scan (two cells per lane),
+// and its chunk-list entries with one lane per chunk.
 __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__restrict__ scenes,
                                                           int n_scenes, Ws ws) {
     __shared__ int4 wsum[8];
+    __shared__ int s_off[kScanTile], s_coff[kScanTile], s_boff[kScanTile], s_cnt[kScanTile];
+    __shared__ int s_list[kScanTile];
+    __shared__ int s_nlist;
     const int tile = blockIdx.x;
     const int b0 = tile * kScanTile + threadIdx.x * kScanPerThread;
-    const int cs = ws.chunk_size;
+    if (threadIdx.x == 0) s_nlist = 0;
     int cnt[kScanPerThread];
     int4 acc = make_int4(0, 0, 0, 0);
 #pragma unroll
@@ -140,49 +147,60 @@ __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__rest
         if (b < ws.nbk) acc = add4(acc, bucket_triple(ws, b, cnt[j]));
     }
     int4 total;
-    int4 inc = cta_scan4(acc, wsum, total);
+    int4 inc = cta_scan4(acc, wsum, total);  // its barriers also order s_nlist = 0
     const int4 pre = ws.tile_sums[tile];
     int off = pre.x + inc.x - acc.x, coff = pre.y + inc.y - acc.y, boff = pre.z + inc.z - acc.z;
 #pragma unroll
     for (int j = 0; j < kScanPerThread; ++j) {
-        int b = b0 + j;
+        const int b = b0 + j;
         if (b >= ws.nbk) break;
         ws.counts[b] = 0;
+        const int li = threadIdx.x * kScanPerThread + j;
+        s_off[li] = off;
+        s_coff[li] = coff;
+        s_boff[li] = boff;
+        s_cnt[li] = cnt[j];
         // the out-of-domain bucket always gets its cursor (its particles sort
         // after every other one; G2P's copy chunks count them again)
-        if (cnt[j] > 0 || b == ws.nbk - 1) {
-            // cell offsets inside the block; zero its cell histogram
-            int4 *cc = reinterpret_cast<int4 *>(ws.cell_counts + (int64_t)b * 64);
-            int4 *cs4 = reinterpret_cast<int4 *>(ws.cell_start + (int64_t)b * 64);
-            int4 *cu4 = reinterpret_cast<int4 *>(ws.cell_cursor + (int64_t)b * 64);
-            int4 k[16];
+        if (cnt[j] > 0 || b == ws.nbk - 1) s_list[atomicAdd(&s_nlist, 1)] = li;
+        const int4 t = bucket_triple(ws, b, cnt[j]);
+        off += t.x;
+        coff += t.y;
+        boff += t.z;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int nlist = s_nlist;
+    const int cs = ws.chunk_size;
+    for (int i = (int)(threadIdx.x >> 5); i < nlist; i += 8) {
+        const int li = s_list[i];
+        const int b = tile * kScanTile + li;
+        const int bo = s_off[li], n_b = s_cnt[li];
+        // cell offsets of the block: lane owns cells 2 lane, 2 lane + 1
+        int2 *cc = reinterpret_cast<int2 *>(ws.cell_counts + (int64_t)b * 64);
+        const int2 k = cc[lane];
+        const int sum = k.x + k.y;
+        int incl = sum;
 #pragma unroll
-            for (int q = 0; q < 16; ++q) k[q] = cc[q];  // all loads in flight at once
-            int run = off;
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int4 st4 = make_int4(run, run + k[q].x, run + k[q].x + k[q].y,
-                                           run + k[q].x + k[q].y + k[q].z);
-                run += k[q].x + k[q].y + k[q].z + k[q].w;
-                cs4[q] = st4;
-                cu4[q] = st4;
-                cc[q] = make_int4(0, 0, 0, 0);
-            }
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
         }
-        if (cnt[j] > 0) {
+        const int st = bo + incl - sum;
+        const int2 st2 = make_int2(st, st + k.x);
+        reinterpret_cast<int2 *>(ws.cell_start + (int64_t)b * 64)[lane] = st2;
+        reinterpret_cast<int2 *>(ws.cell_cursor + (int64_t)b * 64)[lane] = st2;
+        cc[lane] = make_int2(0, 0);
+        if (n_b > 0) {
             const bool real = b < ws.nbk - 1;
             const int sc = real ? scene_of_block(scenes, n_scenes, b) : -1;  // -1: copy chunk
-            if (real) {
-                if (boff < ws.nbk - 1) ws.blocks[boff] = make_int4(b, off, cnt[j], sc);
-                ++boff;
-            }
-            for (int s = 0; s < cnt[j]; s += cs) {
-                if (coff < ws.max_chunks)
-                    ws.chunks[coff] = make_int4(b, off + s, min(cs, cnt[j] - s), sc);
-                ++coff;
+            if (real && lane == 0 && s_boff[li] < ws.nbk - 1) ws.blocks[s_boff[li]] = make_int4(b, bo, n_b, sc);
+            const int nch = (n_b + cs - 1) / cs;
+            for (int c = lane; c < nch; c += 32) {
+                const int at = s_coff[li] + c;
+                if (at < ws.max_chunks) ws.chunks[at] = make_int4(b, bo + c * cs, min(cs, n_b - c * cs), sc);
             }
         }
-        off += cnt[j];
     }
     if (tile == 0 && threadIdx.x == 0) {
         *ws.n_active_prev = *ws.n_active;
@@ -190,23 +208,42 @@ __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__rest
     }
 }
 
-// order[cell_cursor[key]++] = slot, warp-aggregated.  Also zeroes the grid
-// accumulator of the previous substep's active blocks (kept until now so
-// grid mass/momentum stay readable between substeps).
-__global__ void scatter_kernel(PState st, Ws ws, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+// order[cell_cursor[key]++] = slot, warp-aggregated.  Each thread takes
+// kScatterPer keys (strided by the grid's thread count) so that their
+// cursor atomics are in flight together.  Also zeroes the grid accumulator
+// of the previous substep's active blocks (kept until now so grid mass and
+// momentum stay readable between substeps).
+constexpr int kScatterPer = 4;
+
+__global__ void __launch_bounds__(256) scatter_kernel(PState st, Ws ws, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
     const int nclear = *ws.n_active_prev * kBlockNodes;
-    for (int j = i; j < nclear; j += gridDim.x * blockDim.x)
+    for (int j = i; j < nclear; j += stride)
         ws.grid_acc[(int64_t)ws.active_list[j >> 6] * kBlockNodes + (j & 63)] = make_float4(0.f, 0.f, 0.f, 0.f);
-    int key = i < n ? st.key[i] : -1;
-    unsigned peers = __match_any_sync(0xffffffffu, key);
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(peers) - 1;
-    int base = 0;
-    if (key >= 0 && lane == leader) base = atomicAdd(ws.cell_cursor + key, __popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    const int pos = base + __popc(peers & ((1u << lane) - 1u));
-    if (key >= 0 && pos < n) ws.order[pos] = i;
+    const int lane = threadIdx.x & 31;
+    int key[kScatterPer], base[kScatterPer];
+    unsigned peers[kScatterPer];
+#pragma unroll
+    for (int r = 0; r < kScatterPer; ++r) {
+        const int64_t idx = (int64_t)i + (int64_t)r * stride;
+        key[r] = idx < n ? st.key[idx] : -1;
+    }
+#pragma unroll
+    for (int r = 0; r < kScatterPer; ++r) {
+        peers[r] = __match_any_sync(0xffffffffu, key[r]);
+        const int leader = __ffs(peers[r]) - 1;
+        base[r] = 0;
+        if (key[r] >= 0 && lane == leader) base[r] = atomicAdd(ws.cell_cursor + key[r], __popc(peers[r]));
+    }
+#pragma unroll
+    for (int r = 0; r < kScatterPer; ++r) {
+        const int leader = __ffs(peers[r]) - 1;
+        const int b = __shfl_sync(0xffffffffu, base[r], leader);
+        const int pos = b + __popc(peers[r] & ((1u << lane) - 1u));
+        const int64_t idx = (int64_t)i + (int64_t)r * stride;
+        if (key[r] >= 0 && pos < n) ws.order[pos] = (int)idx;
+    }
 }
 
 cudaError_t launch_keys(const Ctx &cx) {
@@ -219,7 +256,8 @@ cudaError_t launch_keys(const Ctx &cx) {
 cudaError_t launch_sort(const Ctx &cx) {
     scan_tiles_kernel<<<cx.ws.n_tiles, 256, 0, cx.stream>>>(cx.ws);
     scan_finish_kernel<<<cx.ws.n_tiles, 256, 0, cx.stream>>>(cx.scenes, cx.n_scenes, cx.ws);
-    const int sgrid = cx.n > 0 ? (cx.n + 255) / 256 : 1;
+    const int per = 256 * kScatterPer;
+    const int sgrid = cx.n > 0 ? (cx.n + per - 1) / per : 1;
     scatter_kernel<<<sgrid, 256, 0, cx.stream>>>(cx.st, cx.ws, cx.n);
     return cudaGetLastError();
 }
