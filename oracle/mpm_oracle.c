@@ -43,10 +43,14 @@
  * det(A) carried by s[2].  In the f64 build the Jacobi rotations are exact
  * and iterated to convergence, so the f64 oracle is an accurate rerun.
  *
- * Parity unpinned: the reference ships no tests, golden vectors or fixtures
- * for this path and cannot run here (it needs warp-lang, which is not
- * installed).  The oracle is checked instead against closed-form known-answer
- * cases and against an independent NumPy/LAPACK restatement.
+ * Pinning: the reference ships no tests, golden vectors or fixtures for this
+ * path, and warp-lang is not installed.  Its unmodified solver
+ * (engine_stress/mpm_solver_warp.py, mpm_utils.py) was therefore run on the
+ * CPU through a test-only stand-in of the Warp API (tests/refshim); the
+ * fixtures it wrote (tests/golden/ref_*.npz, by
+ * tests/golden/make_ref_fixtures.py) pin this oracle substep by substep
+ * (tests/test_ref_fixtures_cpu.py), next to closed-form known-answer cases
+ * and an independent NumPy/LAPACK restatement.
  *
  * Deliberate deviation from the reference (which has undefined behaviour
  * there): a particle whose stencil would leave the grid (base index outside

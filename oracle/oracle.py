@@ -6,8 +6,11 @@ this module; it is the checker, never the thing measured for the GPU path.
 ``OracleSim`` holds the reference's own arrays (engine_stress/mpm_solver_warp.py:52-69:
 AoS vec3 / row-major mat33 per particle, dense (n,n,n) grid) as NumPy arrays
 in float32 or float64 and advances them with the C restatement in
-``mpm_oracle.c``.  Parity is unpinned against the reference itself (no
-golden vectors exist and Warp is not installed); see ``mpm_oracle.c``.
+``mpm_oracle.c``.  Pinned to the reference's own outputs: the reference
+ships no golden vectors and Warp is not installed, so its unmodified solver
+was run on the CPU through a test-only Warp stand-in (``tests/refshim``)
+and the oracle is checked against those runs (``tests/golden/ref_*.npz``,
+``tests/test_ref_fixtures_cpu.py``).
 """
 from __future__ import annotations
 

@@ -13,8 +13,9 @@ namespace mpm {
 constexpr int kTile = 6;                // padded node tile per 4^3-cell block
 constexpr int kTileNodes = kTile * kTile * kTile;  // 216
 constexpr int kBlockNodes = 64;         // nodes of one 4x4x4 grid block
+constexpr int kScanThreads = 256;      // threads per scan CTA
 constexpr int kScanPerThread = 2;      // buckets per scan thread
-constexpr int kScanTile = 256 * kScanPerThread;  // buckets per scan CTA
+constexpr int kScanTile = kScanThreads * kScanPerThread;  // buckets per scan CTA
 constexpr int kSvdSweeps = 5;           // Jacobi sweeps (converged in float32)
 
 // ---------------------------------------------------------------------------
@@ -352,13 +353,17 @@ __device__ __forceinline__ void sym_eig3(const float B[6], float ev[3]) {
         return;
     }
     const float p = sqrtf(p2 * (1.0f / 6.0f));
-    const float ip = 1.0f / p;
+    const float ip = __fdividef(1.0f, p);
     const float c0 = d0 * ip, c1 = B[1] * ip, c2 = B[2] * ip, c3 = d1 * ip, c4 = B[4] * ip, c5 = d2 * ip;
     const float det = c0 * (c3 * c5 - c4 * c4) - c1 * (c1 * c5 - c4 * c2) + c2 * (c1 * c4 - c3 * c2);
     const float r = fminf(fmaxf(0.5f * det, -1.0f), 1.0f);
     const float a = acosf(r) * (1.0f / 3.0f);
-    ev[0] = q + 2.0f * p * cosf(a);
-    ev[2] = q + 2.0f * p * cosf(a + 2.0943951023931953f);
+    // cos(a + 2 pi / 3) = -cos(a) / 2 - sin(a) sqrt(3) / 2; a in [0, pi/3], so
+    // both terms have one sign and nothing cancels
+    float sa, ca;
+    sincosf(a, &sa, &ca);
+    ev[0] = q + 2.0f * p * ca;
+    ev[2] = q - p * (ca + 1.7320508075688772f * sa);
     ev[1] = 3.0f * q - ev[0] - ev[2];
 }
 
@@ -390,16 +395,17 @@ __device__ __forceinline__ void mat_mul(const float A[9], const float B[9], floa
 // takes the SVD path) for inverted or extremely compressed elements.
 // ---------------------------------------------------------------------------
 // log(x / y) / (x - y) for x, y > 0, finite as x -> y
+// (x, y >= 0.01 here, so the fast divisions stay in their exact range)
 __device__ __forceinline__ float log_ratio_div(float x, float y) {
     const float d = x - y;
-    const float u = d / y;
-    if (fabsf(u) < 1e-3f) return (1.0f - u * (0.5f - u * (1.0f / 3.0f))) / y;
-    return log1pf(u) / d;
+    const float u = __fdividef(d, y);
+    if (fabsf(u) < 1e-3f) return __fdividef(1.0f - u * (0.5f - u * (1.0f / 3.0f)), y);
+    return __fdividef(log1pf(u), d);
 }
 // expm1(z) / z, finite at 0
 __device__ __forceinline__ float expm1_div(float z) {
     if (fabsf(z) < 1e-4f) return 1.0f + z * (0.5f + z * (1.0f / 6.0f));
-    return expm1f(z) / z;
+    return __fdividef(expm1f(z), z);
 }
 
 struct Newton3 {
@@ -435,7 +441,7 @@ __device__ __forceinline__ void newton3_eval(const Newton3 &N, float f0, float f
     const float dab = N.iso0 ? d01 : d12;
     const float dbc = N.iso0 ? d12 : d01;
     const float den = N.c - N.a;
-    const float d2 = den != 0.0f ? (dbc - dab) / den : 0.0f;
+    const float d2 = fabsf(den) > 1e-30f ? __fdividef(dbc - dab, den) : 0.0f;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         const float id = (k == 0 || k == 3 || k == 5) ? 1.0f : 0.0f;
@@ -461,9 +467,10 @@ __device__ __forceinline__ bool sand_return_map_spectral(const MpmScene &S, cons
     const float mu = S.mu, lam = S.lam;
     const float e0 = 0.5f * log1pf(ev[0]), e1 = 0.5f * log1pf(ev[1]), e2 = 0.5f * log1pf(ev[2]);
     const float tr = e0 + e1 + e2;
-    const float h0 = e0 - tr / 3.0f, h1 = e1 - tr / 3.0f, h2 = e2 - tr / 3.0f;
+    const float tr3 = tr * (1.0f / 3.0f);
+    const float h0 = e0 - tr3, h1 = e1 - tr3, h2 = e2 - tr3;
     const float hn = sqrtf(h0 * h0 + h1 * h1 + h2 * h2);
-    const float dg = hn + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * S.alpha;
+    const float dg = hn + __fdividef(3.0f * lam + 2.0f * mu, 2.0f * mu) * tr * S.alpha;
     Newton3 N;
     newton3_setup(B, ev, N);
     const float q0 = 1.0f + ev[0], q1 = 1.0f + ev[1], q2 = 1.0f + ev[2];
@@ -493,7 +500,7 @@ __device__ __forceinline__ bool sand_return_map_spectral(const MpmScene &S, cons
     } else {
         // cone: E' = E - r (E - tr/3 I); F = exp(-r (E - tr/3 I)) F_trial,
         // g(beta) = exp(-r (e(beta) - tr/3)), g[x, y] = g(y) expm1(-r (e(x) - e(y))) / (x - y)
-        const float r = dg / hn;
+        const float r = __fdividef(dg, hn);  // hn >= dg > 0 on the cone (tr <= 0)
         const float g0 = expf(-r * h0), g1 = expf(-r * h1), g2 = expf(-r * h2);
         const float z01 = -r * l01, z12 = -r * l12;  // (e(x) - e(y)) = l (x - y)
         const float dg01 = g1 * z01 * expm1_div(z01 * (ev[0] - ev[1]));
@@ -501,7 +508,7 @@ __device__ __forceinline__ bool sand_return_map_spectral(const MpmScene &S, cons
         float Gm[6];
         newton3_eval(N, g0, g2, dg01, dg12, Gm);
         sym_times(Gm, Ft, Fo);
-        const float k1 = 1.0f - r, k0 = r * tr / 3.0f;
+        const float k1 = 1.0f - r, k0 = r * tr3;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             const float id = (k == 0 || k == 3 || k == 5) ? 1.0f : 0.0f;

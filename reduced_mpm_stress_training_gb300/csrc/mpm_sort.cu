@@ -44,9 +44,10 @@ __device__ __forceinline__ int4 add4(int4 a, int4 b) {
     return make_int4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
 
-// inclusive scan of an int4 triple over the 256 threads of a CTA; returns the
-// thread's inclusive value and leaves the CTA total in *total (shared)
-__device__ __forceinline__ int4 cta_scan4(int4 v, int4 *wsum /* [8] shared */, int4 &total) {
+// inclusive scan of an int4 triple over the kScanThreads threads of a CTA;
+// returns the thread's inclusive value and leaves the CTA total in *total
+constexpr int kScanWarps = kScanThreads / 32;
+__device__ __forceinline__ int4 cta_scan4(int4 v, int4 *wsum /* [kScanWarps] shared */, int4 &total) {
     int4 x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -61,7 +62,7 @@ __device__ __forceinline__ int4 cta_scan4(int4 v, int4 *wsum /* [8] shared */, i
     __syncthreads();
     int4 pre = make_int4(0, 0, 0, 0);
     total = make_int4(0, 0, 0, 0);
-    for (int w = 0; w < 8; ++w) {
+    for (int w = 0; w < kScanWarps; ++w) {
         if (w < (int)(threadIdx.x >> 5)) pre = add4(pre, wsum[w]);
         total = add4(total, wsum[w]);
     }
@@ -80,8 +81,8 @@ __device__ __forceinline__ int4 bucket_triple(const Ws &ws, int b, int cnt) {
 // Phase 1: per-tile sums.  The last CTA to finish (atomic ticket; nobody
 // waits) scans the tile sums into exclusive tile offsets and publishes the
 // work-list lengths.
-__global__ void __launch_bounds__(256) scan_tiles_kernel(Ws ws) {
-    __shared__ int4 wsum[8];
+__global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(Ws ws) {
+    __shared__ int4 wsum[kScanWarps];
     __shared__ bool last;
     const int tile = blockIdx.x;
     const int b0 = tile * kScanTile + threadIdx.x * kScanPerThread;
@@ -103,7 +104,7 @@ __global__ void __launch_bounds__(256) scan_tiles_kernel(Ws ws) {
     if (!last) return;
     __threadfence();
     int4 carry = make_int4(0, 0, 0, 0);
-    for (int base = 0; base < ws.n_tiles; base += 256) {
+    for (int base = 0; base < ws.n_tiles; base += kScanThreads) {
         const int t = base + threadIdx.x;
         int4 v = t < ws.n_tiles ? __ldcg(ws.tile_sums + t) : make_int4(0, 0, 0, 0);
         int4 tot;
@@ -129,9 +130,9 @@ __global__ void __launch_bounds__(256) scan_tiles_kernel(Ws ws) {
 // prefix); then the CTA's warps take its non-empty buckets one at a time and
 // write the 64 cell offsets of each with a warp scan (two cells per lane),
 // and its chunk-list entries with one lane per chunk.
-__global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__restrict__ scenes,
+__global__ void __launch_bounds__(kScanThreads) scan_finish_kernel(const MpmScene *__restrict__ scenes,
                                                           int n_scenes, Ws ws) {
-    __shared__ int4 wsum[8];
+    __shared__ int4 wsum[kScanWarps];
     __shared__ int s_off[kScanTile], s_coff[kScanTile], s_boff[kScanTile], s_cnt[kScanTile];
     __shared__ int s_list[kScanTile];
     __shared__ int s_nlist;
@@ -172,7 +173,7 @@ __global__ void __launch_bounds__(256) scan_finish_kernel(const MpmScene *__rest
     const int lane = threadIdx.x & 31;
     const int nlist = s_nlist;
     const int cs = ws.chunk_size;
-    for (int i = (int)(threadIdx.x >> 5); i < nlist; i += 8) {
+    for (int i = (int)(threadIdx.x >> 5); i < nlist; i += kScanWarps) {
         const int li = s_list[i];
         const int b = tile * kScanTile + li;
         const int bo = s_off[li], n_b = s_cnt[li];
@@ -254,8 +255,8 @@ cudaError_t launch_keys(const Ctx &cx) {
 }
 
 cudaError_t launch_sort(const Ctx &cx) {
-    scan_tiles_kernel<<<cx.ws.n_tiles, 256, 0, cx.stream>>>(cx.ws);
-    scan_finish_kernel<<<cx.ws.n_tiles, 256, 0, cx.stream>>>(cx.scenes, cx.n_scenes, cx.ws);
+    scan_tiles_kernel<<<cx.ws.n_tiles, kScanThreads, 0, cx.stream>>>(cx.ws);
+    scan_finish_kernel<<<cx.ws.n_tiles, kScanThreads, 0, cx.stream>>>(cx.scenes, cx.n_scenes, cx.ws);
     const int per = 256 * kScatterPer;
     const int sgrid = cx.n > 0 ? (cx.n + per - 1) / per : 1;
     scatter_kernel<<<sgrid, 256, 0, cx.stream>>>(cx.st, cx.ws, cx.n);

@@ -711,8 +711,20 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
             const int nq = np > 0 ? np * kRecQuads : 0;
             float4 *dst = out.rec + (int64_t)(ch.y + w0) * kRecQuads;
             const float4 *src = sm.outrec + w0 * kOutStride;
-            for (int l = (int)(threadIdx.x & 31u); l < nq; l += 32)
-                dst[l] = src[(l / kRecQuads) * kOutStride + (l % kRecQuads)];
+            // quad l of the warp's run is quad l % 10 of record l / 10, at
+            // (l / 10) * 11 + l % 10 = l + l / 10 in the padded staging; l / 10
+            // advances by 3 or 4 as l advances by 32
+            static_assert(kRecQuads == 10 && kOutStride == 11, "write-out index stepping");
+            int l = (int)(threadIdx.x & 31u), r = l / kRecQuads, q = l - r * kRecQuads;
+            for (; l < nq; l += 32) {
+                dst[l] = src[l + r];
+                q += 2;
+                r += 3;
+                if (q >= kRecQuads) {
+                    q -= kRecQuads;
+                    r += 1;
+                }
+            }
         }
         // outrec is rewritten only after the next iteration's barrier, which
         // every warp reaches after its write-out
