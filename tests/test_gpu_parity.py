@@ -208,7 +208,13 @@ def test_sand_column_32k_rollout(cuda):
     errs64 = compare(sim, ref64)
     spread = {f: rel(getattr(ref, f), getattr(ref64, f)) for f in ("v", "C", "F", "stress")}
     print("gpu vs oracle32", errs, "gpu vs oracle64", errs64, "oracle32 vs oracle64", spread)
-    assert errs["x"] < TOL_ROLLOUT and errs["F"] < TOL_ROLLOUT and errs["v"] < TOL_ROLLOUT
+    # v of the falling column carries the float32 rounding of the stress near F = I: the
+    # float32 oracle itself ends about 9e-5 from the float64 rerun, so against it v has the
+    # per-substep policy's bar (1e-4, or 3x that floor); against the float64 rerun every
+    # field must be within 1e-4
+    assert errs["x"] < TOL_ROLLOUT and errs["F"] < TOL_ROLLOUT
+    assert errs["v"] < max(TOL_ROLLOUT, 3.0 * spread["v"]), (errs, spread)
+    assert all(errs64[f] < TOL_ROLLOUT for f in ("x", "v", "F")), errs64
     g = gpu_state(sim)
     for f in ("stress",):
         ok, info = within_fp32_floor(g[f], getattr(ref, f), getattr(ref64, f), rtol=TOL_ROLLOUT)
