@@ -173,33 +173,51 @@ __global__ void __launch_bounds__(kScanThreads) scan_finish_kernel(const MpmScen
     const int lane = threadIdx.x & 31;
     const int nlist = s_nlist;
     const int cs = ws.chunk_size;
-    for (int i = (int)(threadIdx.x >> 5); i < nlist; i += kScanWarps) {
-        const int li = s_list[i];
-        const int b = tile * kScanTile + li;
-        const int bo = s_off[li], n_b = s_cnt[li];
-        // cell offsets of the block: lane owns cells 2 lane, 2 lane + 1
-        int2 *cc = reinterpret_cast<int2 *>(ws.cell_counts + (int64_t)b * 64);
-        const int2 k = cc[lane];
-        const int sum = k.x + k.y;
-        int incl = sum;
+    // a warp takes kScanPrefetch of the tile's non-empty buckets at a time and
+    // loads all their cell counts before scanning any, so the loads' round
+    // trips overlap instead of queueing one after another
+    constexpr int kScanPrefetch = 8;
+    const int warp = (int)(threadIdx.x >> 5);
+    for (int i0 = warp; i0 < nlist; i0 += kScanWarps * kScanPrefetch) {
+        int lis[kScanPrefetch];
+        int2 ks[kScanPrefetch];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
+        for (int u = 0; u < kScanPrefetch; ++u) {
+            const int i = i0 + u * kScanWarps;
+            lis[u] = i < nlist ? s_list[i] : -1;
+            ks[u] = lis[u] >= 0
+                        ? reinterpret_cast<const int2 *>(ws.cell_counts + (int64_t)(tile * kScanTile + lis[u]) * 64)[lane]
+                        : make_int2(0, 0);
         }
-        const int st = bo + incl - sum;
-        const int2 st2 = make_int2(st, st + k.x);
-        reinterpret_cast<int2 *>(ws.cell_start + (int64_t)b * 64)[lane] = st2;
-        reinterpret_cast<int2 *>(ws.cell_cursor + (int64_t)b * 64)[lane] = st2;
-        cc[lane] = make_int2(0, 0);
-        if (n_b > 0) {
-            const bool real = b < ws.nbk - 1;
-            const int sc = real ? scene_of_block(scenes, n_scenes, b) : -1;  // -1: copy chunk
-            if (real && lane == 0 && s_boff[li] < ws.nbk - 1) ws.blocks[s_boff[li]] = make_int4(b, bo, n_b, sc);
-            const int nch = (n_b + cs - 1) / cs;
-            for (int c = lane; c < nch; c += 32) {
-                const int at = s_coff[li] + c;
-                if (at < ws.max_chunks) ws.chunks[at] = make_int4(b, bo + c * cs, min(cs, n_b - c * cs), sc);
+#pragma unroll
+        for (int u = 0; u < kScanPrefetch; ++u) {
+            const int li = lis[u];
+            if (li < 0) break;  // uniform over the warp
+            const int b = tile * kScanTile + li;
+            const int bo = s_off[li], n_b = s_cnt[li];
+            // cell offsets of the block: lane owns cells 2 lane, 2 lane + 1
+            const int2 k = ks[u];
+            const int sum = k.x + k.y;
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int st = bo + incl - sum;
+            const int2 st2 = make_int2(st, st + k.x);
+            reinterpret_cast<int2 *>(ws.cell_start + (int64_t)b * 64)[lane] = st2;
+            reinterpret_cast<int2 *>(ws.cell_cursor + (int64_t)b * 64)[lane] = st2;
+            reinterpret_cast<int2 *>(ws.cell_counts + (int64_t)b * 64)[lane] = make_int2(0, 0);
+            if (n_b > 0) {
+                const bool real = b < ws.nbk - 1;
+                const int sc = real ? scene_of_block(scenes, n_scenes, b) : -1;  // -1: copy chunk
+                if (real && lane == 0 && s_boff[li] < ws.nbk - 1) ws.blocks[s_boff[li]] = make_int4(b, bo, n_b, sc);
+                const int nch = (n_b + cs - 1) / cs;
+                for (int c = lane; c < nch; c += 32) {
+                    const int at = s_coff[li] + c;
+                    if (at < ws.max_chunks) ws.chunks[at] = make_int4(b, bo + c * cs, min(cs, n_b - c * cs), sc);
+                }
             }
         }
     }
@@ -219,17 +237,18 @@ constexpr int kScatterPer = 4;
 __global__ void __launch_bounds__(256) scatter_kernel(PState st, Ws ws, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
-    const int nclear = *ws.n_active_prev * kBlockNodes;
-    for (int j = i; j < nclear; j += stride)
-        ws.grid_acc[(int64_t)ws.active_list[j >> 6] * kBlockNodes + (j & 63)] = make_float4(0.f, 0.f, 0.f, 0.f);
     const int lane = threadIdx.x & 31;
     int key[kScatterPer], base[kScatterPer];
     unsigned peers[kScatterPer];
+    // the keys' loads first, so their round trip overlaps the clearing below
 #pragma unroll
     for (int r = 0; r < kScatterPer; ++r) {
         const int64_t idx = (int64_t)i + (int64_t)r * stride;
-        key[r] = idx < n ? st.key[idx] : -1;
+        key[r] = idx < n ? __ldcs(st.key + idx) : -1;
     }
+    const int nclear = *ws.n_active_prev * kBlockNodes;
+    for (int j = i; j < nclear; j += stride)
+        ws.grid_acc[(int64_t)ws.active_list[j >> 6] * kBlockNodes + (j & 63)] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int r = 0; r < kScatterPer; ++r) {
         peers[r] = __match_any_sync(0xffffffffu, key[r]);

@@ -208,3 +208,28 @@ def build_simulator(sc: Scene, device="cuda:0", chunk_size: int = 128):
         else:
             sim.add_bounding_box(**kw)
     return sim
+
+
+def run(name: str, substeps: int, device="cuda:0") -> dict:
+    """Build a named scene and take `substeps` plain substeps on the device
+    (the driver the ncu summaries profile); returns the wall time per substep
+    and the status word."""
+    import time
+
+    import torch
+
+    sc = SCENES[name]()
+    sim = build_simulator(sc, device=device)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    for k in range(substeps):
+        sim.p2g2p(k, sc.dt)
+    torch.cuda.synchronize(device)
+    return {"scene": name, "substeps": substeps, "ms_per_substep": 1e3 * (time.perf_counter() - t0) / max(substeps, 1),
+            "status": int(sim.check_status())}
+
+
+if __name__ == "__main__":
+    import sys
+
+    print(run(sys.argv[1] if len(sys.argv) > 1 else "sand_column_1m", int(sys.argv[2]) if len(sys.argv) > 2 else 12))
