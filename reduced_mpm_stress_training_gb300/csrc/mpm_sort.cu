@@ -139,6 +139,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_finish_kernel(const MpmScen
     const int tile = blockIdx.x;
     const int b0 = tile * kScanTile + threadIdx.x * kScanPerThread;
     if (threadIdx.x == 0) s_nlist = 0;
+    const int4 pre = ws.tile_sums[tile];  // loaded beside the counts: one round trip for both
     int cnt[kScanPerThread];
     int4 acc = make_int4(0, 0, 0, 0);
 #pragma unroll
@@ -149,7 +150,6 @@ __global__ void __launch_bounds__(kScanThreads) scan_finish_kernel(const MpmScen
     }
     int4 total;
     int4 inc = cta_scan4(acc, wsum, total);  // its barriers also order s_nlist = 0
-    const int4 pre = ws.tile_sums[tile];
     int off = pre.x + inc.x - acc.x, coff = pre.y + inc.y - acc.y, boff = pre.z + inc.z - acc.z;
 #pragma unroll
     for (int j = 0; j < kScanPerThread; ++j) {
