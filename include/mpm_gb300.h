@@ -424,6 +424,13 @@ int mpm_mlp_forward_tc(const void *params, const float *x, float *y, const float
  * MPM_MLP_PARAMS).  work: 2*n*128 bf16 scratch. */
 int mpm_mlp_backward(const void *params, const float *x, const void *zsave, const void *dy, void *work,
                      float *grad, int64_t n, void *stream);
+/* The same backward on the tcgen05 tensor cores: one persistent CTA per SM
+ * holds the four weight gradients in tensor memory over all of its 128-row
+ * tiles and adds them, with the bias sums, into grad once at the end (no
+ * scratch).  err: one device int32 the kernel ORs 1 into if a tensor-core
+ * completion wait ran out (grad then incomplete); the caller zeroes it. */
+int mpm_mlp_backward_tc(const void *params, const float *x, const void *zsave, const void *dy, float *grad,
+                        int64_t n, int32_t *err, void *stream);
 /* One Adam step (torch.optim.Adam semantics, step >= 1) on the fp32
  * master parameters; rewrites the bf16/fp32 blob params from them. */
 int mpm_mlp_adam(float *master, float *m, float *v, const float *grad, void *params, float lr,

@@ -138,6 +138,8 @@ _SIGS = {
                             C.c_void_p, C.c_float, C.c_int64, C.c_void_p, C.c_void_p], C.c_int),
     "mpm_mlp_backward": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                           C.c_int64, C.c_void_p], C.c_int),
+    "mpm_mlp_backward_tc": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                             C.c_void_p, C.c_void_p], C.c_int),
     "mpm_mlp_adam": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
                       C.c_float, C.c_float, C.c_float, C.c_int32, C.c_void_p], C.c_int),
     "mpm_surrogate_features": ([C.POINTER(MpmScene), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

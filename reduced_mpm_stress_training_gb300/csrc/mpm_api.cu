@@ -488,6 +488,17 @@ int mpm_mlp_forward_tc(const void *params, const float *x, float *y, const float
     return MPM_OK;
 }
 
+int mpm_mlp_backward_tc(const void *params, const float *x, const void *zsave, const void *dy, float *grad,
+                        int64_t n, int32_t *err, void *stream) {
+    if (!params || !err || !grad || n < 0 || (n > 0 && (!x || !zsave || !dy))) return MPM_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(params) & 15 || reinterpret_cast<uintptr_t>(grad) & 15 ||
+        reinterpret_cast<uintptr_t>(zsave) & 15 || reinterpret_cast<uintptr_t>(dy) & 15)
+        return MPM_ERR_ARG;
+    MPM_CHECK(mpm::launch_mlp_backward_tc(params, x, zsave, dy, grad, n, err, num_sms(),
+                                          static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
 int mpm_surrogate_apply(const MpmScene *scene, const void *mlp_params, const MpmSurrogateConfig *cfg,
                         const float *F_trial, float *F, float *stress, int32_t *codes, int64_t n, void *stream) {
     if (!scene || !mlp_params || !surrogate_cfg_ok(cfg) || n < 0) return MPM_ERR_ARG;

@@ -61,6 +61,10 @@ int64_t mlp_tc_smem_bytes();
 cudaError_t launch_mlp_forward_tc(const void *params, const float *x, float *y, const float *target, void *zsave,
                                   void *dy, float *loss, float grad_scale, int64_t n, int *err, int num_sms,
                                   cudaStream_t stream);
+// tcgen05 network backward (mpm_mlp_bw_tc.cu)
+int64_t mlp_bw_tc_smem_bytes();
+cudaError_t launch_mlp_backward_tc(const void *params, const float *x, const void *zsave, const void *dy,
+                                   float *grad, int64_t n, int *err, int num_sms, cudaStream_t stream);
 cudaError_t launch_features(const MpmScene &scene, const float *F, const float *stress, float *x, float *y,
                             int64_t n, cudaStream_t stream);
 

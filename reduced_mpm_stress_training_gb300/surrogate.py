@@ -58,8 +58,9 @@ class StressMLP:
 
     def __init__(self, device="cuda:0", seed: int = 0, master: np.ndarray | None = None,
                  tensor_memory: bool = True):
-        """tensor_memory: run the forward on the tcgen05 tensor cores
-        (mpm_mlp_forward_tc) instead of the mma.sync kernel."""
+        """tensor_memory: run the forward and the backward on the tcgen05
+        tensor cores (mpm_mlp_forward_tc, mpm_mlp_backward_tc) instead of the
+        mma.sync kernels."""
         self.lib = A.load()
         self.tensor_memory = bool(tensor_memory)
         if self.lib.mpm_mlp_param_bytes() != W_COUNT * 2 + (P_COUNT - W_COUNT) * 4:
@@ -128,9 +129,9 @@ class StressMLP:
                                              _ptr(dy), _ptr(loss), grad_scale, n, st), "mpm_mlp_forward")
 
     def check_tensor_cores(self) -> None:
-        """Raise if a tensor-core completion wait of the forward ever ran out."""
+        """Raise if a tensor-core completion wait of the forward or backward ever ran out."""
         if int(self.tc_error.item()):
-            raise RuntimeError("tcgen05 forward: a tensor-core completion wait timed out")
+            raise RuntimeError("tcgen05 network kernels: a tensor-core completion wait timed out")
 
     def loss_and_grad(self, x: torch.Tensor, target: torch.Tensor, accumulate: bool = False,
                       grad_scale: float | None = None) -> torch.Tensor:
@@ -146,8 +147,13 @@ class StressMLP:
         self.loss.zero_()
         st = _stream(self.device)
         self._forward(x, None, target, b["z"], b["dy"], self.loss, grad_scale, n)
-        A.check(self.lib.mpm_mlp_backward(_ptr(self.params), _ptr(x), _ptr(b["z"]), _ptr(b["dy"]),
-                                          _ptr(b["work"]), _ptr(self.grad), n, st), "mpm_mlp_backward")
+        if self.tensor_memory:
+            A.check(self.lib.mpm_mlp_backward_tc(_ptr(self.params), _ptr(x), _ptr(b["z"]), _ptr(b["dy"]),
+                                                 _ptr(self.grad), n, _ptr(self.tc_error), st),
+                    "mpm_mlp_backward_tc")
+        else:
+            A.check(self.lib.mpm_mlp_backward(_ptr(self.params), _ptr(x), _ptr(b["z"]), _ptr(b["dy"]),
+                                              _ptr(b["work"]), _ptr(self.grad), n, st), "mpm_mlp_backward")
         return self.loss / (n * OUT)
 
     def adam(self, lr: float = 1e-3, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8) -> None:

@@ -105,3 +105,32 @@ def test_tcgen05_forward_matches_oracle(cuda, n):
     assert rel(yg, ref) < 2e-3, rel(yg, ref)
     y2 = net.forward(xt).cpu().numpy()
     assert rel(yg, y2) < 2e-3
+
+
+@pytest.mark.parametrize("n", [1, 127, 128, 1000, 5000, 70000])
+def test_tcgen05_backward_matches_mma_sync_and_oracle(cuda, n):
+    """The tcgen05 / tensor-memory backward (weight gradients held in tensor
+    memory over a CTA's tiles) against the mma.sync backward on the same
+    forward outputs, and against the oracle: every weight and bias gradient."""
+    x, t = _data(n, 31 + n)
+    xt, tt = torch.from_numpy(x).to(cuda), torch.from_numpy(t).to(cuda)
+    grads = {}
+    for name, tc in (("tcgen05", True), ("mma_sync", False)):
+        net = StressMLP(cuda, seed=13, tensor_memory=tc)
+        net.loss_and_grad(xt, tt)
+        torch.cuda.synchronize()
+        net.check_tensor_cores()
+        grads[name] = net.grad.cpu().numpy()
+        p = net.master.cpu().numpy()
+    o = M.forward(p, x, t, 2.0 / (n * M.OUT))
+    g_ref = M.backward(p, o["cache"])
+    gw, gb = M.unpack(grads["tcgen05"])
+    sw, sb = M.unpack(grads["mma_sync"])
+    rw, rb = M.unpack(g_ref)
+    for l in range(4):
+        assert np.isfinite(gw[l]).all() and np.isfinite(gb[l]).all()
+        assert rel(gw[l], sw[l]) < 5e-3, ("W vs mma.sync", l, rel(gw[l], sw[l]))
+        assert rel(gb[l], sb[l]) < 5e-3, ("b vs mma.sync", l, rel(gb[l], sb[l]))
+        assert rel(gw[l], rw[l]) < 1e-2, ("W vs oracle", l, rel(gw[l], rw[l]))
+        assert rel(gb[l], rb[l]) < 1e-2, ("b vs oracle", l, rel(gb[l], rb[l]))
+    assert np.all(gw[0][:, M.IN:] == 0) and np.all(gw[3][M.OUT:, :] == 0) and np.all(gb[3][M.OUT:] == 0)
