@@ -250,7 +250,12 @@ def surrogate_extra(device) -> dict:
             "stress_rel_l2_vs_plain": err["rel_l2"],
             "accepted_fraction": acc / n, "outcomes": counts,
             "training": {"tuples": 8_000_000, "steps": 60000, "batch": 65536, "seconds": round(t_train, 1),
-                         "data_seconds": round(t1 - t0, 1), "loss": log[-1][1]}}
+                         "data_seconds": round(t1 - t0, 1), "loss": log[-1][1],
+                         "kernels": "tcgen05 forward and backward (tensor-memory accumulators), Adam",
+                         # forward 2 (12*128 + 2*128*128 + 128*6) flop per row, the backward twice that
+                         "tflops": round(3 * 2.0 * (12 * 128 + 2 * 128 * 128 + 128 * 6) * 65536 * 60000
+                                         / t_train / 1e12, 1),
+                         "peak_tflops": measured_peak_bf16()}}
 
 
 def dist_env():
@@ -343,6 +348,18 @@ def measured_peak_hbm():
         return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, copy)"
     except Exception:
         return 6800.0, "fallback (6.8 TB/s)"
+
+
+def measured_peak_bf16():
+    """Dense bf16 TFLOP/s: the burst figure (a kernel timed alone) and the
+    sustained one (a kernel inside a long loop), from MEASURED_PEAKS.json."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return {"burst": float(d["bf16_tflops"]), "sustained": float(d["bf16_tflops_sustained"]),
+                "source": "measured (MEASURED_PEAKS.json, cuBLAS bf16)"}
+    except Exception:
+        return {"burst": 1900.0, "sustained": 1700.0, "source": "fallback"}
 
 
 def profiled_traffic(workload: str):

@@ -59,26 +59,40 @@ __device__ __forceinline__ void st_bf16(unsigned char *base, uint32_t off, float
     *reinterpret_cast<__nv_bfloat16 *>(base + off) = __float2bfloat16_rn(v);
 }
 
-// W_l [out][in] row-major (the blob) -> W_l^T as a K-major B operand [in][K = out]
+// W_l [out][in] row-major (the blob) -> W_l^T as a K-major B operand [in][K = out];
+// eight weights per 16-byte load
 __device__ __forceinline__ void stage_wt(unsigned char *dst, const __nv_bfloat16 *w, int n_out, int slab_bytes) {
-    for (int i = threadIdx.x; i < n_out * H; i += blockDim.x) {
-        const int o = i / H, in = i % H;
-        *reinterpret_cast<__nv_bfloat16 *>(dst + elem_off(in, o, slab_bytes)) = w[i];
+    for (int i = threadIdx.x; i < n_out * (H / 8); i += blockDim.x) {
+        const int o = i / (H / 8), in0 = (i % (H / 8)) * 8;
+        const uint4 v = reinterpret_cast<const uint4 *>(w)[i];
+        const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) *reinterpret_cast<__nv_bfloat16 *>(dst + elem_off(in0 + j, o, slab_bytes)) = e[j];
     }
 }
 
-// H_{l-1}^T from the saved pre-activations Z_{l-1} of this thread's row
-// (columns [c0, c0 + 64)): H = bf16(silu(Z)), written transposed
-__device__ __forceinline__ void stage_ht(BwSmem &s, const __nv_bfloat16 *zrow, int row, int c0) {
-#pragma unroll 1
-    for (int c = c0; c < c0 + 64; c += 8) {
-        uint4 v = zrow ? *reinterpret_cast<const uint4 *>(zrow + c) : make_uint4(0u, 0u, 0u, 0u);
-        const uint32_t *u = reinterpret_cast<const uint32_t *>(&v);
+// this thread's 64 columns [c0, c0 + 64) of a saved pre-activation row (zeros past n)
+struct ZHalf {
+    uint4 v[8];
+};
+__device__ __forceinline__ void load_zhalf(ZHalf &z, const __nv_bfloat16 *zrow, int c0) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        z.v[q] = zrow ? *reinterpret_cast<const uint4 *>(zrow + c0 + 8 * q) : make_uint4(0u, 0u, 0u, 0u);
+}
+
+// H_{l-1}^T from the pre-activations Z_{l-1} of this thread's row (columns
+// [c0, c0 + 64)): H = bf16(silu(Z)), written transposed
+__device__ __forceinline__ void stage_ht(BwSmem &s, const ZHalf &z, int row, int c0) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t *u = reinterpret_cast<const uint32_t *>(&z.v[q]);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             const float2 zz = unpack_bf16(u[e]);
-            st_bf16(s.ht, elem_off(c + 2 * e, row, kSlab), silu(zz.x));
-            st_bf16(s.ht, elem_off(c + 2 * e + 1, row, kSlab), silu(zz.y));
+            const int c = c0 + 8 * q + 2 * e;
+            st_bf16(s.ht, elem_off(c, row, kSlab), silu(zz.x));
+            st_bf16(s.ht, elem_off(c + 1, row, kSlab), silu(zz.y));
         }
     }
 }
@@ -169,9 +183,12 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_backward_tc_kernel(const __nv
                 *reinterpret_cast<__nv_bfloat16 *>(s.dz4t + elem_off(c + 8, row, kW4Slab)) = dv1[c];
             }
         }
-        const __nv_bfloat16 *z3 = valid ? zsave + 2 * n * H + grow * H : nullptr;
-        const __nv_bfloat16 *z2 = valid ? zsave + 1 * n * H + grow * H : nullptr;
-        const __nv_bfloat16 *z1 = valid ? zsave + grow * H : nullptr;
+        // the row's three saved pre-activations (this thread's half), loaded
+        // together up front so one round trip serves the whole tile
+        ZHalf z3, z2, z1;
+        load_zhalf(z3, valid ? zsave + 2 * n * H + grow * H : nullptr, half * 64);
+        load_zhalf(z2, valid ? zsave + 1 * n * H + grow * H : nullptr, half * 64);
+        load_zhalf(z1, valid ? zsave + grow * H : nullptr, half * 64);
         stage_ht(s, z3, row, half * 64);
         bw_sync();
         if (tid < N4) db4 += sum_row_t(s.dz4t, tid, kW4Slab);
@@ -185,25 +202,25 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_backward_tc_kernel(const __nv
         }
         if (!(ok = bw_wait(s, phase))) break;
         // ---- layers 3, 2: dZ_l = dH_l * silu'(Z_l); then dgrad + wgrad of layer l ----
-#pragma unroll 1
+#pragma unroll
         for (int l = 3; l >= 2; --l) {
-            const __nv_bfloat16 *zl = l == 3 ? z3 : z2;  // Z_l of this row
-            const __nv_bfloat16 *zp = l == 3 ? z2 : z1;  // Z_{l-1}: H_{l-1}^T for dW_l
-#pragma unroll 1
-            for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
+            const ZHalf &zl = l == 3 ? z3 : z2;  // Z_l of this row
+            const ZHalf &zp = l == 3 ? z2 : z1;  // Z_{l-1}: H_{l-1}^T for dW_l
+#pragma unroll
+            for (int h2 = 0; h2 < 2; ++h2) {
+                const int c0 = half * 64 + 32 * h2;
                 float acc[32];
                 tmem_ld32(tlane + C_DH + (uint32_t)c0, acc);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    uint4 zv = zl ? *reinterpret_cast<const uint4 *>(zl + c0 + 8 * q) : make_uint4(0u, 0u, 0u, 0u);
-                    const uint32_t *zu = reinterpret_cast<const uint32_t *>(&zv);
+                    const uint32_t *zu = reinterpret_cast<const uint32_t *>(&zl.v[4 * h2 + q]);
                     uint32_t dv[4];
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
                         const float2 zz = unpack_bf16(zu[e]);
                         const int c = q * 8 + 2 * e;
-                        const float g0 = zl ? acc[c] * silu_grad(zz.x) : 0.0f;
-                        const float g1 = zl ? acc[c + 1] * silu_grad(zz.y) : 0.0f;
+                        const float g0 = valid ? acc[c] * silu_grad(zz.x) : 0.0f;
+                        const float g1 = valid ? acc[c + 1] * silu_grad(zz.y) : 0.0f;
                         dv[e] = pack_bf16(g0, g1);
                         const float2 r = unpack_bf16(dv[e]);  // the bf16 values, for the transpose
                         st_bf16(s.dzt, elem_off(c0 + c, row, kSlab), r.x);
@@ -233,20 +250,20 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_backward_tc_kernel(const __nv
         }
         if (!ok) break;
         // ---- layer 1: dZ1 = dH1 * silu'(Z1); dW1 += dZ1^T x ----
-#pragma unroll 1
-        for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+            const int c0 = half * 64 + 32 * h2;
             float acc[32];
             tmem_ld32(tlane + C_DH + (uint32_t)c0, acc);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                uint4 zv = z1 ? *reinterpret_cast<const uint4 *>(z1 + c0 + 8 * q) : make_uint4(0u, 0u, 0u, 0u);
-                const uint32_t *zu = reinterpret_cast<const uint32_t *>(&zv);
+                const uint32_t *zu = reinterpret_cast<const uint32_t *>(&z1.v[4 * h2 + q]);
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const float2 zz = unpack_bf16(zu[e]);
                     const int c = q * 8 + 2 * e;
-                    const float g0 = z1 ? acc[c] * silu_grad(zz.x) : 0.0f;
-                    const float g1 = z1 ? acc[c + 1] * silu_grad(zz.y) : 0.0f;
+                    const float g0 = valid ? acc[c] * silu_grad(zz.x) : 0.0f;
+                    const float g1 = valid ? acc[c + 1] * silu_grad(zz.y) : 0.0f;
                     st_bf16(s.dzt, elem_off(c0 + c, row, kSlab), g0);
                     st_bf16(s.dzt, elem_off(c0 + c + 1, row, kSlab), g1);
                 }
