@@ -418,12 +418,61 @@ def time_forward(rows: int = 1 << 20, device="cuda:0", reps: int = 20) -> dict:
     return out
 
 
+def time_training_step(rows: int = 65536, device="cuda:0", reps: int = 50) -> dict:
+    """Milliseconds of the forward (with loss gradient), the backward and the
+    Adam step on a batch of ``rows`` rows, tcgen05 and mma.sync kernels, CUDA
+    events; the backward's TFLOP/s counts 2 x the forward's flops."""
+    dev = torch.device(device)
+    g = torch.Generator(device=dev).manual_seed(0)
+    x = torch.randn(rows, IN, generator=g, device=dev)
+    t = torch.tanh(torch.randn(rows, OUT, generator=g, device=dev))
+    flops_fwd = 2.0 * rows * (IN * HID + HID * HID * 2 + HID * OUT)
+    out = {}
+    for name, tc in (("tcgen05", True), ("mma_sync", False)):
+        net = StressMLP(dev, seed=0, tensor_memory=tc)
+        for _ in range(3):
+            net.train_step(x, t)
+        b = net._buffers(rows)
+        st = torch.cuda.current_stream(dev)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        acc = [0.0, 0.0, 0.0]
+        for _ in range(reps):
+            net.grad.zero_()
+            net.loss.zero_()
+            ev[0].record(st)
+            net._forward(x, None, t, b["z"], b["dy"], net.loss, 2.0 / (rows * OUT), rows)
+            ev[1].record(st)
+            if tc:
+                A.check(net.lib.mpm_mlp_backward_tc(_ptr(net.params), _ptr(x), _ptr(b["z"]), _ptr(b["dy"]),
+                                                    _ptr(net.grad), rows, _ptr(net.tc_error), st.cuda_stream),
+                        "mpm_mlp_backward_tc")
+            else:
+                A.check(net.lib.mpm_mlp_backward(_ptr(net.params), _ptr(x), _ptr(b["z"]), _ptr(b["dy"]),
+                                                 _ptr(b["work"]), _ptr(net.grad), rows, st.cuda_stream),
+                        "mpm_mlp_backward")
+            ev[2].record(st)
+            net.adam(1e-3)
+            ev[3].record(st)
+            torch.cuda.synchronize(dev)
+            for i in range(3):
+                acc[i] += ev[i].elapsed_time(ev[i + 1]) / reps
+        net.check_tensor_cores()
+        out[name] = {"forward_ms": acc[0], "backward_ms": acc[1], "adam_ms": acc[2],
+                     "backward_tflops": 2.0 * flops_fwd / (acc[1] * 1e-3) / 1e12}
+    return out
+
+
 if __name__ == "__main__":
     import argparse
     import json
 
-    ap = argparse.ArgumentParser(description="time the stress-network forward kernels")
+    ap = argparse.ArgumentParser(description="time the stress-network kernels")
     ap.add_argument("--rows", type=int, default=1 << 20)
     ap.add_argument("--reps", type=int, default=20)
+    ap.add_argument("--training", action="store_true",
+                    help="time a training step (forward, backward, Adam) instead of the forward")
     a = ap.parse_args()
-    print(json.dumps(time_forward(a.rows, reps=a.reps)))
+    if a.training:
+        print(json.dumps(time_training_step(a.rows, reps=a.reps)))
+    else:
+        print(json.dumps(time_forward(a.rows, reps=a.reps)))
