@@ -17,6 +17,7 @@
 // the parameters (zero-padded to HP neurons) sit in shared memory and are
 // read as broadcasts, the activations stay in registers.
 #include "mpm_launch.h"
+#include "mpm_mlp_tc.cuh"
 
 namespace mpm {
 
@@ -256,6 +257,255 @@ __global__ void __launch_bounds__(kDecThreads) decoder_stress_kernel(MpmStressDe
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core form of decoder_stress_kernel for widths up to 32 (the
+// reference's default is 30).  The four 32 x 32 hidden layers carry 85 % of the
+// multiply-adds.  They run as tcgen05 MMAs on 128-particle tiles, with FP32
+// accumulators in tensor memory.
+//
+// FP32 accuracy comes from BF16 operands: every activation and weight is
+// split exactly into three BF16 pieces (x = x0 + x1 + x2, 8 significant bits
+// each).  The six products x_i w_j with i + j <= 2 are accumulated, smallest
+// first.  Each of the three dropped products is below 2^-24 |x| |w|.
+//
+// Layer 0 stays on the CUDA cores: the label's part once per CTA, then the
+// position and mu columns per particle.  The 6-wide output layer does too.
+//
+// One thread per tile row (TMEM lane).  Each layer's epilogue (bias,
+// activation, split into the next layer's A operand) runs on the CUDA cores
+// between the MMAs.  Every mbarrier wait is bounded; a timeout sets
+// MPM_ST_INTERNAL and the CTA stops.
+// ---------------------------------------------------------------------------
+namespace dtc {
+
+constexpr int kRows = 128;              // particles per tile = TMEM lanes = threads
+constexpr int kHP = 32;                 // padded width
+constexpr int kParts = 3;               // BF16 pieces per FP32 value
+constexpr int kASlab = kRows * 16 * 2;  // one 128 x 16 BF16 K slab (4 KB)
+constexpr int kWSlab = kHP * 16 * 2;    // one 32 x 16 BF16 K slab (1 KB)
+constexpr int kKSlabs = kHP / 16;
+constexpr uint32_t kTmemCols = 32;
+constexpr int kMaxCols = 3 + 4;         // per-particle layer-0 columns: position + mu
+
+struct Smem {
+    alignas(128) unsigned char a[kParts][kKSlabs * kASlab];     // the tile's activations
+    alignas(128) unsigned char w[4][kParts][kKSlabs * kWSlab];  // hidden-layer weights
+    alignas(16) float w0p[kMaxCols][kHP];  // layer 0, position and mu columns, [k][j]
+    alignas(16) float c0[kHP];             // layer-0 bias + the label's part
+    alignas(16) float bh[4][kHP];
+    alignas(16) float we[6][kHP];
+    float be[6], prep[6], qm[6], qs[6];
+    alignas(8) unsigned long long mbar;
+    uint32_t tmem_base;
+};
+
+// two values -> their three BF16 pieces, packed in pairs (exact: each
+// difference is representable in FP32, the last one in BF16)
+__device__ __forceinline__ void split3(float x, float y, uint32_t &p0, uint32_t &p1, uint32_t &p2) {
+    p0 = mlp::pack_bf16(x, y);
+    const float2 f0 = mlp::unpack_bf16(p0);
+    const float rx = __fsub_rn(x, f0.x), ry = __fsub_rn(y, f0.y);
+    p1 = mlp::pack_bf16(rx, ry);
+    const float2 f1 = mlp::unpack_bf16(p1);
+    p2 = mlp::pack_bf16(__fsub_rn(rx, f1.x), __fsub_rn(ry, f1.y));
+}
+
+// row's 32 activations -> the three A operands (K-major core-matrix layout)
+__device__ __forceinline__ void store_row(Smem &s, int row, const float v[kHP]) {
+#pragma unroll
+    for (int q = 0; q < kHP / 8; ++q) {
+        uint32_t h0[4], h1[4], h2[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) split3(v[q * 8 + 2 * e], v[q * 8 + 2 * e + 1], h0[e], h1[e], h2[e]);
+        const uint32_t off = mlptc::chunk_off(row, q, kASlab);
+        *reinterpret_cast<uint4 *>(s.a[0] + off) = make_uint4(h0[0], h0[1], h0[2], h0[3]);
+        *reinterpret_cast<uint4 *>(s.a[1] + off) = make_uint4(h1[0], h1[1], h1[2], h1[3]);
+        *reinterpret_cast<uint4 *>(s.a[2] + off) = make_uint4(h2[0], h2[1], h2[2], h2[3]);
+    }
+}
+
+// the parameters: hidden weights as BF16 pieces, the rest FP32, zero-padded to 32
+__device__ void stage(const MpmStressDecoder &d, const float *label, Smem &s) {
+    const int h = d.hidden, L0 = d.label_dim, M = d.mu_dim, in = L0 + 3 + M;
+    const BlobLayout B = blob_layout(h, in);
+    const float *P = d.params;
+    for (int i = threadIdx.x; i < 4 * kHP * kHP; i += blockDim.x) {
+        const int l = i / (kHP * kHP), j = (i / kHP) % kHP, k = i % kHP;
+        const float w = (j < h && k < h) ? P[B.wh + (l * h + j) * h + k] : 0.0f;
+        const __nv_bfloat16 b0 = __float2bfloat16_rn(w);
+        const float r = __fsub_rn(w, __bfloat162float(b0));
+        const __nv_bfloat16 b1 = __float2bfloat16_rn(r);
+        const __nv_bfloat16 b2 = __float2bfloat16_rn(__fsub_rn(r, __bfloat162float(b1)));
+        const uint32_t off = mlptc::chunk_off(j, k >> 3, kWSlab) + (k & 7) * 2;
+        *reinterpret_cast<__nv_bfloat16 *>(s.w[l][0] + off) = b0;
+        *reinterpret_cast<__nv_bfloat16 *>(s.w[l][1] + off) = b1;
+        *reinterpret_cast<__nv_bfloat16 *>(s.w[l][2] + off) = b2;
+    }
+    for (int i = threadIdx.x; i < kMaxCols * kHP; i += blockDim.x) {
+        const int k = i / kHP, j = i % kHP;
+        s.w0p[k][j] = (j < h && k < 3 + M) ? P[B.w0 + j * in + L0 + k] : 0.0f;
+    }
+    for (int j = threadIdx.x; j < kHP; j += blockDim.x) {
+        float acc = j < h ? P[B.b0 + j] : 0.0f;
+        for (int k = 0; k < L0 && j < h; ++k) acc = fmaf(P[B.w0 + j * in + k], label[k], acc);
+        s.c0[j] = acc;
+    }
+    for (int i = threadIdx.x; i < 4 * kHP; i += blockDim.x) {
+        const int l = i / kHP, j = i % kHP;
+        s.bh[l][j] = j < h ? P[B.bh + l * h + j] : 0.0f;
+    }
+    for (int i = threadIdx.x; i < 6 * kHP; i += blockDim.x) {
+        const int c = i / kHP, j = i % kHP;
+        s.we[c][j] = j < h ? P[B.we + c * h + j] : 0.0f;
+    }
+    for (int i = threadIdx.x; i < 6; i += blockDim.x) {
+        s.be[i] = P[B.be + i];
+        s.prep[i] = P[B.prep + i];
+        s.qm[i] = P[B.qm + i];
+        s.qs[i] = P[B.qs + i];
+    }
+}
+
+}  // namespace dtc
+
+__global__ void __launch_bounds__(dtc::kRows) decoder_stress_tc_kernel(MpmStressDecoder d, PState st,
+                                                                      const float *__restrict__ label,
+                                                                      const float *__restrict__ mu, int n,
+                                                                      int *status) {
+    using namespace dtc;
+    extern __shared__ __align__(128) unsigned char dtc_smem_raw[];
+    Smem &s = *reinterpret_cast<Smem *>(dtc_smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int M = d.mu_dim;
+    const bool siren = d.siren != 0;
+    stage(d, label, s);
+    if (tid == 0) {
+        const uint32_t a = (uint32_t)__cvta_generic_to_shared(&s.mbar);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(a) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s.tmem_base);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(dst),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    mlptc::fence_async_smem();
+    mlptc::tc_before_sync();
+    __syncthreads();
+    mlptc::tc_after_sync();
+    const uint32_t tbase = s.tmem_base;
+    const uint32_t tlane = tbase + ((uint32_t)(warp * 32) << 16);
+    const uint32_t id = mlptc::idesc_bf16(kRows, kHP);
+    // the six piece products, smallest first: (activation piece, weight piece)
+    constexpr int kPa[6] = {2, 1, 0, 1, 0, 0}, kPw[6] = {0, 1, 2, 0, 1, 0};
+    uint32_t phase = 0;
+    bool ok = true;
+    const int n_tiles = (n + kRows - 1) / kRows;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const int i = tile * kRows + tid;
+        const bool live = i < n;
+        // layer 0 (dec0 + act): the label part is in c0; position and mu per particle
+        float xin[kMaxCols];
+#pragma unroll
+        for (int k = 0; k < kMaxCols; ++k) xin[k] = 0.0f;
+        if (live) {
+            const float4 q0 = ldrec(st, i, 0), q1 = ldrec(st, i, 1);
+            xin[0] = dec_prep(s.prep, 0, q0.x, siren);
+            xin[1] = dec_prep(s.prep, 1, q0.y, siren);
+            xin[2] = dec_prep(s.prep, 2, q0.z, siren);
+            const int uid = __float_as_int(q1.y);
+#pragma unroll
+            for (int k = 0; k < kMaxCols - 3; ++k)
+                if (k < M) xin[3 + k] = mu[(int64_t)uid * M + k];
+        }
+        float h[kHP];
+#pragma unroll
+        for (int j = 0; j < kHP; ++j) h[j] = s.c0[j];
+#pragma unroll
+        for (int k = 0; k < kMaxCols; ++k) {
+            if (k >= 3 + M) break;
+            const float4 *w4 = reinterpret_cast<const float4 *>(s.w0p[k]);
+#pragma unroll
+            for (int q = 0; q < kHP / 4; ++q) {
+                const float4 w = w4[q];
+                h[4 * q + 0] = fmaf(w.x, xin[k], h[4 * q + 0]);
+                h[4 * q + 1] = fmaf(w.y, xin[k], h[4 * q + 1]);
+                h[4 * q + 2] = fmaf(w.z, xin[k], h[4 * q + 2]);
+                h[4 * q + 3] = fmaf(w.w, xin[k], h[4 * q + 3]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kHP; ++j) h[j] = dec_act(h[j], siren, d.omega_0);
+        store_row(s, tid, h);
+        // dec1..dec4 + act on the tensor cores
+        for (int l = 0; l < 4; ++l) {
+            mlptc::fence_async_smem();
+            mlptc::tc_before_sync();
+            __syncthreads();
+            mlptc::tc_after_sync();
+            if (tid == 0) {
+                bool acc = false;
+#pragma unroll
+                for (int t = 0; t < 6; ++t)
+#pragma unroll
+                    for (int ks = 0; ks < kKSlabs; ++ks) {
+                        mlptc::mma_bf16(tbase, mlptc::smem_desc(s.a[kPa[t]] + ks * kASlab),
+                                        mlptc::smem_desc(s.w[l][kPw[t]] + ks * kWSlab), id, acc);
+                        acc = true;
+                    }
+                mlptc::mma_commit(&s.mbar);
+            }
+            ok = __syncthreads_and(mlptc::mbar_wait(&s.mbar, phase) ? 1 : 0) != 0;
+            phase ^= 1u;
+            mlptc::tc_after_sync();
+            if (!ok) break;  // uniform
+            float acc[kHP];
+            mlptc::tmem_ld32(tlane, acc);
+#pragma unroll
+            for (int j = 0; j < kHP; ++j) h[j] = dec_act(acc[j] + s.bh[l][j], siren, d.omega_0);
+            // the layer's MMAs are done reading the A operands: overwrite them
+            if (l < 3) store_row(s, tid, h);
+            mlptc::tc_before_sync();
+        }
+        if (!ok) break;
+        // enc + invStandardizeQ
+        float q[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            float acc = s.be[c];
+            const float4 *w4 = reinterpret_cast<const float4 *>(s.we[c]);
+#pragma unroll
+            for (int k = 0; k < kHP / 4; ++k) {
+                const float4 w = w4[k];
+                acc = fmaf(w.x, h[4 * k + 0], acc);
+                acc = fmaf(w.y, h[4 * k + 1], acc);
+                acc = fmaf(w.z, h[4 * k + 2], acc);
+                acc = fmaf(w.w, h[4 * k + 3], acc);
+            }
+            q[c] = __fadd_rn(s.qm[c], __fmul_rn(acc, s.qs[c]));
+        }
+        if (live) {
+            const float4 q5 = ldrec(st, i, 5);
+            strec(st, i, 5, make_float4(q5.x, q5.y, q5.z, q[0]));
+            strec(st, i, 6, make_float4(q[1], q[2], q[1], q[3]));
+            strec(st, i, 7, make_float4(q[4], q[2], q[4], q[5]));
+        }
+    }
+    if (!ok && tid == 0) atomicOr(status, MPM_ST_INTERNAL);
+    // tear-down: after a timed-out wait the MMAs may still run; give them a
+    // bounded grace period before the tensor memory is released
+    mlptc::tc_before_sync();
+    __syncthreads();
+    mlptc::tc_after_sync();
+    if (warp == 0) {
+        if (!ok) mlptc::mbar_wait(&s.mbar, phase ^ 1u);
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tbase), "r"(kTmemCols)
+                     : "memory");
+    }
+}
+
 int64_t decoder_param_floats(const MpmStressDecoder &d) {
     return blob_layout(d.hidden, d.label_dim + 3 + d.mu_dim).total;
 }
@@ -307,8 +557,21 @@ cudaError_t launch_decoder_stress(const Ctx &cx, const MpmStressDecoder &d, cons
     const int grid = want < cx.num_sms * 8 ? want : cx.num_sms * 8;
     cudaError_t e;
     if (dec_hp(d.hidden) == 32) {
-        if ((e = dec_prepare(decoder_stress_kernel<32>, 2)) != cudaSuccess) return e;
-        decoder_stress_kernel<32><<<grid, kDecThreads, smem, cx.stream>>>(d, cx.st, label, mu, cx.n);
+        // tensor cores: persistent CTAs, four per SM (about 50 KB of shared memory
+        // and 32 tensor-memory columns each)
+        static bool attr[64];
+        int dev = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+        const int bytes = (int)sizeof(dtc::Smem);
+        if (!attr[dev]) {
+            e = cudaFuncSetAttribute(decoder_stress_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            if (e != cudaSuccess) return e;
+            attr[dev] = true;
+        }
+        const int tiles = (cx.n + dtc::kRows - 1) / dtc::kRows;
+        const int tgrid = tiles < cx.num_sms * 4 ? tiles : cx.num_sms * 4;
+        decoder_stress_tc_kernel<<<tgrid, dtc::kRows, bytes, cx.stream>>>(d, cx.st, label, mu, cx.n, cx.status);
     } else {
         if ((e = dec_prepare(decoder_stress_kernel<64>, 3)) != cudaSuccess) return e;
         decoder_stress_kernel<64><<<grid, kDecThreads, smem, cx.stream>>>(d, cx.st, label, mu, cx.n);
