@@ -36,6 +36,20 @@ def test_stress_components_round_trip():
     assert np.array_equal(FR.stress_from_components(comps), S)  # the reader's expansion (:283-292)
 
 
+def test_stress_component_order_is_the_references():
+    """Stated independently of the library's own index table: the six stored
+    components are [xx, xy, xz, yy, yz, zz] (mpm_solver_warp.py:383 keeps
+    flattened indices 0, 1, 2, 4, 5, 8), one row per component, (6, n)."""
+    T = np.array([[1.0, 2.0, 3.0], [2.0, 4.0, 5.0], [3.0, 5.0, 6.0]], np.float32)
+    comps = T.reshape(1, 9)[:, list(FR.STRESS_COMPONENTS)]
+    assert comps.tolist() == [[1.0, 2.0, 3.0, 4.0, 5.0, 6.0]]
+    n = 3
+    buf = np.zeros(34 * n, np.float32)
+    buf[16 * n:22 * n] = np.repeat(np.arange(1.0, 7.0, dtype=np.float32), n)  # as the export kernel lays it out
+    assert FR.split_frame_buffer(buf, n)["stress"][:, 0].tolist() == [1.0, 2.0, 3.0, 4.0, 5.0, 6.0]
+    assert np.array_equal(FR.stress_from_components(comps)[0], T)
+
+
 def test_store_round_trip_and_resolve(tmp_path, monkeypatch):
     rng = np.random.default_rng(1)
     data = {"x": rng.random((3, 4)).astype(np.float32), "time": np.array([[0.25]]),

@@ -93,6 +93,7 @@ def test_decoded_stress_feeds_the_substep(cuda):
                                   dict(label_dim=6, scale_mlp=10, mu_dim=1, siren=True),
                                   dict(label_dim=0, scale_mlp=3, mu_dim=2, siren=False),
                                   dict(label_dim=16, scale_mlp=2, mu_dim=0, siren=True),
+                                  dict(label_dim=64, scale_mlp=10, mu_dim=4, siren=False),
                                   dict(label_dim=6, scale_mlp=20, mu_dim=1, siren=False)])
 def test_decoded_stress_matches_float64_for_each_width(cuda, case):
     """mpm_decoder_stress against the float64 restatement on (label, x_initial,
