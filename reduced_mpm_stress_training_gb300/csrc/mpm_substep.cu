@@ -529,10 +529,15 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
     extern __shared__ __align__(16) unsigned char g2p_smem_raw[];
     G2PSmem<CH> &sm = *reinterpret_cast<G2PSmem<CH> *>(g2p_smem_raw);
     const int n_chunks = *ws.n_chunks;
+    // The chunk list is walked from its end.  P2G has just streamed the records
+    // in ascending block order, so the highest positions are the ones still in
+    // L2; and the records written last here (the lowest positions) are the
+    // first that the next substep's P2G reads.  Measured 207.2 -> 203.7 us per
+    // substep on the 1M column against walking it from the start.
     const int sentinel = (ws.nbk - 1) * 64;  // out-of-domain cell key
     int c = blockIdx.x;
     if (c >= n_chunks) return;
-    int4 ch = ws.chunks[c];
+    int4 ch = ws.chunks[n_chunks - 1 - c];
     int slot = g2p_slot(ws, ch);
     g2p_prefetch<CH>(scenes, st, ws, ch, slot, sm, 0);
     cp_async_commit();
@@ -540,7 +545,7 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
     int4 chn = make_int4(0, 0, 0, -1);
     int slotn = 0;
     if (cn < n_chunks) {
-        chn = ws.chunks[cn];
+        chn = ws.chunks[n_chunks - 1 - cn];
         slotn = g2p_slot(ws, chn);
     }
     int buf = 0;
@@ -552,7 +557,7 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
         int4 chnn = make_int4(0, 0, 0, -1);
         int slotnn = 0;
         if (cnn < n_chunks) {
-            chnn = ws.chunks[cnn];
+            chnn = ws.chunks[n_chunks - 1 - cnn];
             slotnn = g2p_slot(ws, chnn);
         }
         cp_async_wait1();
