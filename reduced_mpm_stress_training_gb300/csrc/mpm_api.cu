@@ -101,11 +101,16 @@ int64_t mpm::substep_workspace_bytes(const MpmPlan &p) { return ws_layout(p).sta
 
 namespace {
 
+// [quads 0-3 of every slot][quads 4-7][quads 8-9][cell keys]; stride is a
+// multiple of 64 slots, so every array starts 4 KB-aligned
 mpm::PState state_view(void *base, int64_t stride) {
     mpm::PState s;
+    char *p = static_cast<char *>(base);
     s.stride = stride;
-    s.rec = static_cast<float4 *>(base);
-    s.key = reinterpret_cast<int *>(static_cast<char *>(base) + stride * mpm::kRecWords * 4);
+    s.a = reinterpret_cast<float4 *>(p);
+    s.b = reinterpret_cast<float4 *>(p + stride * 64);
+    s.f = reinterpret_cast<float4 *>(p + stride * 128);
+    s.key = reinterpret_cast<int *>(p + stride * mpm::kRecWords * 4);
     return s;
 }
 

@@ -24,20 +24,24 @@ constexpr int kSvdSweeps = 5;           // Jacobi sweeps (converged in float32)
 // ---------------------------------------------------------------------------
 // Views of the caller's buffers (layout fixed by mpm_plan).
 // ---------------------------------------------------------------------------
-// One particle-state buffer: a 160-byte record per slot (10 float4) plus a
-// cell-key array.  Record words (float unless noted):
-//   q0:  0-2 x_initial, 3 mass
+// One particle-state buffer: a particle's 160-byte record (10 float4 quads)
+// split over three arrays -- quads 0-3 (64 B), 4-7 (64 B) and 8-9 (32 B) per
+// slot -- plus a cell-key array.  Record words (float unless noted):
+//   q0:  0-2 x_initial, 3 mass                                    array a
 //   q1:  4 vol, 5 uid (int bits, the user's particle index), 6 yield_stress, 7 F[8]
 //   q2:  8-10 u, 11 v.x
 //   q3:  12-13 v.y v.z, 14-15 C[0..1]
-//   q4:  16-19 C[2..5]
+//   q4:  16-19 C[2..5]                                            array b
 //   q5:  20-22 C[6..8], 23 stress[0]
 //   q6:  24-27 stress[1..4]
 //   q7:  28-31 stress[5..8]
-//   q8:  32-35 F[0..3]
+//   q8:  32-35 F[0..3]                                            array f
 //   q9:  36-39 F[4..7]
-// P2G reads q0-q7 (128 B, four 32-byte sectors); G2P reads q0, q1, q2, q8,
-// q9 and writes q1-q9.  Matrices are row-major as in the reference.
+// P2G reads q0-q7: one aligned 64-byte piece of a and one of b, so DRAM moves
+// exactly what it reads.  G2P reads q0, q1, q2 (one 64-byte piece of a) and
+// q8, q9 (32 B of f) and writes all three.  In one 160-byte array, each
+// kernel's partial reads dragged in nearly the whole record.  Matrices are
+// row-major as in the reference.
 constexpr int kRecWords = 40;
 constexpr int kRecQuads = 10;
 namespace rec {
@@ -45,19 +49,23 @@ constexpr int X0 = 0, MASS = 3, VOL = 4, UID = 5, YLD = 6, F8 = 7, U = 8, V = 11
               TAU = 23, F0 = 32;
 }
 struct PState {
-    float4 *rec;  // n records (padded stride)
+    float4 *a;    // quads 0-3 of each slot (padded stride)
+    float4 *b;    // quads 4-7
+    float4 *f;    // quads 8-9
     int *key;     // cell key (block * 64 + cell in block) of each slot for the coming sort
     int64_t stride;
 };
 
-__device__ __forceinline__ float4 ldrec(const PState &st, int slot, int q) {
-    return st.rec[(int64_t)slot * kRecQuads + q];
+// address of record quad q (0..9) of a slot
+__device__ __forceinline__ float4 *recq(const PState &st, int slot, int q) {
+    return q < 4 ? st.a + (int64_t)slot * 4 + q
+                 : (q < 8 ? st.b + (int64_t)slot * 4 + (q - 4) : st.f + (int64_t)slot * 2 + (q - 8));
 }
-__device__ __forceinline__ void strec(const PState &st, int slot, int q, float4 v) {
-    st.rec[(int64_t)slot * kRecQuads + q] = v;
-}
-__device__ __forceinline__ float *recw(const PState &st, int slot) {
-    return reinterpret_cast<float *>(st.rec + (int64_t)slot * kRecQuads);
+__device__ __forceinline__ float4 ldrec(const PState &st, int slot, int q) { return *recq(st, slot, q); }
+__device__ __forceinline__ void strec(const PState &st, int slot, int q, float4 v) { *recq(st, slot, q) = v; }
+// record word w (0..39) of a slot
+__device__ __forceinline__ float &recword(const PState &st, int slot, int w) {
+    return reinterpret_cast<float *>(recq(st, slot, w >> 2))[w & 3];
 }
 
 struct Ws {  // workspace

@@ -36,12 +36,16 @@ __device__ __forceinline__ int field_word(int field, int c) {
 __global__ void init_state_kernel(PState a, PState b, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float *ra = recw(a, i), *rb = recw(b, i);
-    for (int k = 0; k < kRecWords; ++k) { ra[k] = 0.0f; rb[k] = 0.0f; }
-    ra[rec::F0] = ra[rec::F0 + 4] = ra[rec::F8] = 1.0f;
-    rb[rec::F0] = rb[rec::F0 + 4] = rb[rec::F8] = 1.0f;
-    ra[rec::UID] = __int_as_float(i);
-    rb[rec::UID] = __int_as_float(i);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < kRecQuads; ++q) {
+        strec(a, i, q, z);
+        strec(b, i, q, z);
+    }
+    recword(a, i, rec::F0) = recword(a, i, rec::F0 + 4) = recword(a, i, rec::F8) = 1.0f;
+    recword(b, i, rec::F0) = recword(b, i, rec::F0 + 4) = recword(b, i, rec::F8) = 1.0f;
+    recword(a, i, rec::UID) = __int_as_float(i);
+    recword(b, i, rec::UID) = __int_as_float(i);
     a.key[i] = -1;
     b.key[i] = -1;
 }
@@ -49,19 +53,17 @@ __global__ void init_state_kernel(PState a, PState b, int n) {
 __global__ void load_kernel(PState st, int n, int field, int nc, const float *__restrict__ src) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float *r = recw(st, i);
-    const int64_t u = __float_as_int(r[rec::UID]);
-    for (int c = 0; c < nc; ++c) r[field_word(field, c)] = src[u * nc + c];
+    const int64_t u = __float_as_int(recword(st, i, rec::UID));
+    for (int c = 0; c < nc; ++c) recword(st, i, field_word(field, c)) = src[u * nc + c];
 }
 
 __global__ void export_kernel(PState st, int n, int field, int nc, float *__restrict__ dst) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float *r = recw(st, i);
-    const int64_t u = __float_as_int(r[rec::UID]);
+    const int64_t u = __float_as_int(recword(st, i, rec::UID));
     for (int c = 0; c < nc; ++c) {
-        float v = r[field_word(field, c)];
-        if (field == MPM_FIELD_X) v = __fadd_rn(v, r[rec::U + c]);                 // x0 + u (:5-7)
+        float v = recword(st, i, field_word(field, c));
+        if (field == MPM_FIELD_X) v = __fadd_rn(v, recword(st, i, rec::U + c));    // x0 + u (:5-7)
         if (field == MPM_FIELD_F_DISP) v = v - ((c % 4 == 0) ? 1.0f : 0.0f);       // F - I (:16-19)
         dst[u * nc + c] = v;
     }

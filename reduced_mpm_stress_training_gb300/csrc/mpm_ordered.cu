@@ -31,7 +31,7 @@ constexpr int64_t kAlignBytes = 256;
 inline int64_t align_up(int64_t x) { return (x + kAlignBytes - 1) / kAlignBytes * kAlignBytes; }
 
 __device__ __forceinline__ int rec_uid(const PState &st, int slot) {
-    return __float_as_int(st.rec[(int64_t)slot * kRecQuads + 1].y);
+    return __float_as_int(ldrec(st, slot, 1).y);
 }
 
 // one thread per (work-list block, cell): insertion sort of the cell's range

@@ -291,7 +291,6 @@ __global__ void __launch_bounds__(128) g2p_sample_kernel(const MpmScene *__restr
     }
     const int N = g.n_grid;
     const int slot = slot_of_uid[p];
-    float *r = recw(st, slot);
     const float4 q0 = ldrec(st, slot, 0), q2 = ldrec(st, slot, 2);
     float gp[3];
     gp[0] = grid_coord(q0.x, q2.x, S.inv_dx);
@@ -342,14 +341,14 @@ __global__ void __launch_bounds__(128) g2p_sample_kernel(const MpmScene *__restr
         u[d] = __fsub_rn(x, x0[d]);  // :469
     }
     const float4 q8 = ldrec(st, slot, 8), q9 = ldrec(st, slot, 9);
-    const float Fo_[9] = {q8.x, q8.y, q8.z, q8.w, q9.x, q9.y, q9.z, q9.w, r[rec::F8]};
+    const float Fo_[9] = {q8.x, q8.y, q8.z, q8.w, q9.x, q9.y, q9.z, q9.w, recword(st, slot, rec::F8)};
     float A[9], Ft[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) A[k] = ((k % 4 == 0) ? 1.0f : 0.0f) + dt * nF[k];
     mat_mul(A, Fo_, Ft);
     float yld = 0.0f;
-    float *ry = metal ? recw(st, slot_of_uid[s]) : nullptr;
-    if (metal) yld = ry[rec::YLD];
+    const int yslot = metal ? slot_of_uid[s] : 0;
+    if (metal) yld = recword(st, yslot, rec::YLD);
     float Fn[9], tau[9];
     if (S.material == MPM_JELLY) {
 #pragma unroll
@@ -357,20 +356,20 @@ __global__ void __launch_bounds__(128) g2p_sample_kernel(const MpmScene *__restr
     } else {
         return_map_stress(S, Ft, yld, Fn, tau);
     }
-    if (metal && S.hardening == 1) ry[rec::YLD] = yld;
+    if (metal && S.hardening == 1) recword(st, yslot, rec::YLD) = yld;
     bool finite = true;
 #pragma unroll
     for (int k = 0; k < 9; ++k) finite = finite && isfinite(Fn[k]);
     if (!finite) atomicOr(status, MPM_ST_NONFINITE);
-    r[rec::U + 0] = u[0];
-    r[rec::U + 1] = u[1];
-    r[rec::U + 2] = u[2];
-    r[rec::V + 0] = nv[0];
-    r[rec::V + 1] = nv[1];
-    r[rec::V + 2] = nv[2];
+    recword(st, slot, rec::U + 0) = u[0];
+    recword(st, slot, rec::U + 1) = u[1];
+    recword(st, slot, rec::U + 2) = u[2];
+    recword(st, slot, rec::V + 0) = nv[0];
+    recword(st, slot, rec::V + 1) = nv[1];
+    recword(st, slot, rec::V + 2) = nv[2];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) r[rec::F0 + k] = Fn[k];
-    r[rec::F8] = Fn[8];
+    for (int k = 0; k < 8; ++k) recword(st, slot, rec::F0 + k) = Fn[k];
+    recword(st, slot, rec::F8) = Fn[8];
     float *fd = g.f_disp + (int64_t)p * 9;
 #pragma unroll
     for (int k = 0; k < 9; ++k) fd[k] = Fn[k] - ((k % 4 == 0) ? 1.0f : 0.0f);  // :471

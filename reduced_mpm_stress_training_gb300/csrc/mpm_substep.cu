@@ -198,9 +198,8 @@ __device__ __forceinline__ void p2g_cp_async16(void *smem, const void *gmem) {
 // queue the copy of one record (slot >= 0) into the lane's buffer b
 __device__ __forceinline__ void p2g_prefetch(P2GWarpSmem &sm, const PState &st, int slot, int b, int lane, int n) {
     if (slot >= 0 && slot < n) {
-        const float4 *src = st.rec + (int64_t)slot * kRecQuads;
 #pragma unroll
-        for (int q = 0; q < kP2GQuads; ++q) p2g_cp_async16(&sm.rec[b][q][lane], src + q);
+        for (int q = 0; q < kP2GQuads; ++q) p2g_cp_async16(&sm.rec[b][q][lane], recq(st, slot, q));
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
@@ -501,7 +500,7 @@ __device__ __forceinline__ void g2p_prefetch(const MpmScene *__restrict__ scenes
     if ((int)threadIdx.x < ch.z && ch.y + (int)threadIdx.x < ws.n) {
 #pragma unroll
         for (int q = 0; q < kG2PQuads; ++q)
-            cp_async16(&sm.rec[b][q][threadIdx.x], st.rec + (int64_t)slot * kRecQuads + g2p_quad(q), 16);
+            cp_async16(&sm.rec[b][q][threadIdx.x], recq(st, slot, g2p_quad(q)), 16);
     }
     const MpmScene &S = scenes[ch.w];
     int bx, by, bz;
@@ -711,27 +710,20 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
         // every warp is done with buffer `buf` (the next iteration prefetches into it)
         __syncthreads();
         if (ch.w >= 0) {
-            // each warp writes its own 32 records (contiguous in `out`) with coalesced
-            // float4 stores
+            // each warp writes its own 32 records, contiguous in each of the
+            // three arrays, with coalesced float4 stores: quads 0-3 to a and
+            // 4-7 to b (four per record), quads 8-9 to f (two per record)
             const int w0 = (int)(threadIdx.x & ~31u);
-            const int np = min(min(32, ch.z - w0), ws.n - ch.y - w0);
-            const int nq = np > 0 ? np * kRecQuads : 0;
-            float4 *dst = out.rec + (int64_t)(ch.y + w0) * kRecQuads;
+            const int np = max(0, min(min(32, ch.z - w0), ws.n - ch.y - w0));
+            const int64_t p0 = (int64_t)ch.y + w0;
             const float4 *src = sm.outrec + w0 * kOutStride;
-            // quad l of the warp's run is quad l % 10 of record l / 10, at
-            // (l / 10) * 11 + l % 10 = l + l / 10 in the padded staging; l / 10
-            // advances by 3 or 4 as l advances by 32
-            static_assert(kRecQuads == 10 && kOutStride == 11, "write-out index stepping");
-            int l = (int)(threadIdx.x & 31u), r = l / kRecQuads, q = l - r * kRecQuads;
-            for (; l < nq; l += 32) {
-                dst[l] = src[l + r];
-                q += 2;
-                r += 3;
-                if (q >= kRecQuads) {
-                    q -= kRecQuads;
-                    r += 1;
-                }
+            const int lane = (int)(threadIdx.x & 31u);
+            for (int l = lane; l < 4 * np; l += 32) {
+                const float4 *rq = src + (l >> 2) * kOutStride + (l & 3);
+                out.a[p0 * 4 + l] = rq[0];
+                out.b[p0 * 4 + l] = rq[4];
             }
+            for (int l = lane; l < 2 * np; l += 32) out.f[p0 * 2 + l] = src[(l >> 1) * kOutStride + 8 + (l & 1)];
         }
         // outrec is rewritten only after the next iteration's barrier, which
         // every warp reaches after its write-out

@@ -243,23 +243,20 @@ struct SurSmem {
 };
 
 __device__ __forceinline__ void ld_F(const PState &st, int pos, float F[9]) {
-    const float4 *r = st.rec + (int64_t)pos * kRecQuads;
-    const float4 a = r[8], b = r[9];
-    const float f8 = reinterpret_cast<const float *>(r + 1)[3];
+    const float4 a = ldrec(st, pos, 8), b = ldrec(st, pos, 9);
+    const float f8 = recword(st, pos, rec::F8);
     F[0] = a.x; F[1] = a.y; F[2] = a.z; F[3] = a.w;
     F[4] = b.x; F[5] = b.y; F[6] = b.z; F[7] = b.w;
     F[8] = f8;
 }
 
 __device__ __forceinline__ void st_F_tau(const PState &st, int pos, const float F[9], const float t[9]) {
-    float4 *r = st.rec + (int64_t)pos * kRecQuads;
-    float *w = reinterpret_cast<float *>(r);
-    w[7] = F[8];
-    w[rec::TAU] = t[0];
-    r[6] = make_float4(t[1], t[2], t[3], t[4]);
-    r[7] = make_float4(t[5], t[6], t[7], t[8]);
-    r[8] = make_float4(F[0], F[1], F[2], F[3]);
-    r[9] = make_float4(F[4], F[5], F[6], F[7]);
+    recword(st, pos, rec::F8) = F[8];
+    recword(st, pos, rec::TAU) = t[0];
+    strec(st, pos, 6, make_float4(t[1], t[2], t[3], t[4]));
+    strec(st, pos, 7, make_float4(t[5], t[6], t[7], t[8]));
+    strec(st, pos, 8, make_float4(F[0], F[1], F[2], F[3]));
+    strec(st, pos, 9, make_float4(F[4], F[5], F[6], F[7]));
 }
 
 // One warp, 32 particles of one sand scene (lane = particle, F of the lane
@@ -476,14 +473,13 @@ __global__ void fallback_kernel(const MpmScene *__restrict__ scenes, PState st, 
         const MpmScene &S = scenes[e.y];
         float F[9], Fo[9], tau[9];
         ld_F(st, e.x, F);
-        float *w = recw(st, e.x);
-        float yld = w[6];
+        float yld = recword(st, e.x, rec::YLD);
         return_map_stress(S, F, yld, Fo, tau);
         float chk = 0.0f;
 #pragma unroll
         for (int k = 0; k < 9; ++k) chk += fabsf(Fo[k]) + fabsf(tau[k]);
         if (!isfinite(chk)) atomicOr(status, MPM_ST_NONFINITE);
-        if (S.material == MPM_METAL && S.hardening == 1) w[6] = yld;
+        if (S.material == MPM_METAL && S.hardening == 1) recword(st, e.x, rec::YLD) = yld;
         st_F_tau(st, e.x, Fo, tau);
     }
 }
