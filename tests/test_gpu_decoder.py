@@ -117,6 +117,24 @@ def test_decoded_stress_matches_float64_for_each_width(cuda, case):
     assert rel(got, OD.symmetric_stress(q64)) <= TOL, (dec.hidden, rel(got, OD.symmetric_stress(q64)))
 
 
+@pytest.mark.parametrize("n", [1, 100, 129])
+def test_decoded_stress_with_fewer_particles_than_two_tiles(cuda, n):
+    """The tensor-core stress decoder with one CTA whose second tile pipeline
+    has no tile (n <= 128) or only a 1-row tile (n = 129): every particle's
+    stress still matches float64."""
+    sc = S.small_column(n, 16)
+    sim = gpu_sim(sc)
+    dec = D.StressDecoder.random(seed=9, x_stats=_stats(False), q_stats=Q_STATS, device=cuda)
+    label = np.random.default_rng(3).normal(0, 1, 6).astype(np.float32)
+    sim.load_stress_from_decoder(dec, torch.from_numpy(label))
+    assert sim.check_status() == 0
+    x0, _, _, _ = sc.particles()
+    rows = np.concatenate([np.tile(label, (n, 1)), x0, np.full((n, 1), sc.friction_angle, np.float32)], 1)
+    q64 = OD.forward(dec.params.cpu().numpy(), rows, 6, 1, dec.hidden, False, 30.0)
+    got = sim.mpm_state.particle_stress.cpu().numpy().reshape(n, 9)
+    assert rel(got, OD.symmetric_stress(q64)) <= TOL
+
+
 def test_decoder_arguments_are_checked(cuda):
     sc = S.small_column(1024, 16)
     sim = gpu_sim(sc)
