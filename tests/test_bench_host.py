@@ -43,3 +43,18 @@ def test_reference_arm_prints_one_json_line(built):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_profiled_traffic_is_consistent():
+    """The per-substep DRAM traffic that bench.py reports as roofline.traffic
+    (an ncu capture of one substep) is the sum of its kernels' reads and
+    writes, and above the algorithmic bytes it is compared with."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    t = bench.profiled_traffic("sand_column_1m")
+    assert t is not None
+    total = sum(k["dram_read_MB"] + k["dram_write_MB"] for k in t["kernels"].values()) * 1e6
+    assert abs(total - t["bytes_per_substep"]) < 1e-3 * t["bytes_per_substep"]
+    assert t["algorithmic_bytes_per_substep"] == 284 * 1048576
+    assert t["bytes_per_substep"] > t["algorithmic_bytes_per_substep"]
