@@ -464,7 +464,6 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // three velocity components: x, y as a pair for the two-wide FP32 FMA, z alone
@@ -549,8 +548,6 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
     }
     int buf = 0;
     while (c < n_chunks) {
-        if (cn < n_chunks) g2p_prefetch<CH>(scenes, st, ws, chn, slotn, sm, buf ^ 1);
-        cp_async_commit();
         // order[] indices two chunks ahead
         const int cnn = cn + gridDim.x;
         int4 chnn = make_int4(0, 0, 0, -1);
@@ -559,8 +556,14 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
             chnn = ws.chunks[n_chunks - 1 - cnn];
             slotnn = g2p_slot(ws, chnn);
         }
-        cp_async_wait1();
+        // this chunk's records and tile have landed, for every thread; and every
+        // warp is done with the other half of the buffer (the previous chunk),
+        // so the next chunk's copies may go there now -- the only CTA-wide
+        // barrier of the iteration
+        cp_async_wait0();
         __syncthreads();
+        if (cn < n_chunks) g2p_prefetch<CH>(scenes, st, ws, chn, slotn, sm, buf ^ 1);
+        cp_async_commit();
 
         const int pos = ch.y + (int)threadIdx.x;
         const bool mine = (int)threadIdx.x < ch.z && pos < ws.n;
@@ -707,8 +710,8 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
             }
         }
         warp_histogram(ws.counts, ws.cell_counts, key);
-        // every warp is done with buffer `buf` (the next iteration prefetches into it)
-        __syncthreads();
+        // each warp writes out the records its own lanes staged
+        __syncwarp();
         if (ch.w >= 0) {
             // each warp writes its own 32 records, contiguous in each of the
             // three arrays, with coalesced float4 stores: quads 0-3 to a and
@@ -725,8 +728,8 @@ __global__ void __launch_bounds__(CH) g2p_kernel(const MpmScene *__restrict__ sc
             }
             for (int l = lane; l < 2 * np; l += 32) out.f[p0 * 2 + l] = src[(l >> 1) * kOutStride + 8 + (l & 1)];
         }
-        // outrec is rewritten only after the next iteration's barrier, which
-        // every warp reaches after its write-out
+        // outrec and this half of the buffer are rewritten only after the next
+        // iteration's barrier, which every warp reaches after its write-out
         c = cn; ch = chn; slot = slotn;
         cn = cnn; chn = chnn; slotn = slotnn;
         buf ^= 1;
